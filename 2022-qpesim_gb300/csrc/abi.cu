@@ -1,0 +1,784 @@
+// abi.cu - implementation of the C ABI declared in include/qpe_gb300.h.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/qpe_gb300.h"
+#include "kernels.h"
+#include "program_build.h"
+#include "qpe_common.h"
+
+namespace qpe {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+#define QPE_CK(expr)                                                                              \
+  do {                                                                                            \
+    cudaError_t e_ = (expr);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      throw ::qpe::Error(e_ == cudaErrorNoDevice || e_ == cudaErrorInsufficientDriver             \
+                             ? QPE_ERR_NO_DEVICE                                                  \
+                             : (e_ == cudaErrorMemoryAllocation ? QPE_ERR_NOMEM : QPE_ERR_CUDA),  \
+                         std::string(#expr) + ": " + cudaGetErrorString(e_));                     \
+  } while (0)
+
+// Device buffer with RAII release.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void alloc(size_t n) {
+    release();
+    if (n == 0) n = 16;
+    QPE_CK(cudaMalloc(&p, n));
+    bytes = n;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+__global__ void k_set_int(int* p, int v) { *p = v; }
+
+}  // namespace qpe
+
+using namespace qpe;
+
+struct qpe_context {
+  int device = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf binom;
+  DevBuf flush;
+  cudaEvent_t events[16] = {};
+};
+
+struct qpe_program {
+  qpe_context* ctx = nullptr;
+  uint64_t id = 0;  // unique per process, keys the cached evolution graphs
+  HostProgram hp;
+  DevBuf pool, ops, coef, strA, strB, tabs, start;
+};
+
+struct qpe_state {
+  qpe_context* ctx = nullptr;
+  uint32_t M = 0, na = 0, nb = 0, P = 0;
+  int dtype = QPE_C128;
+  uint64_t Ca = 0, Cb = 0, ld = 0, N = 0;
+  size_t esz = 16;
+  DevBuf data, work, dk, partial, probs, tw;
+  uint32_t qift_T = 1, qift_grid = 1;
+  bool probs_valid = false;
+  // Cached one-power graph for the last program evolved on this state.
+  uint64_t graph_prog = 0;
+  cudaGraphExec_t graph = nullptr;
+  ~qpe_state() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
+
+namespace qpe {
+
+static void use_device(qpe_context* ctx) { QPE_CK(cudaSetDevice(ctx->device)); }
+
+static void check_ctx(qpe_context* ctx) {
+  if (!ctx) throw Error(QPE_ERR_INVALID, "null context");
+  use_device(ctx);
+}
+
+static void state_alloc(qpe_state* st) {
+  st->esz = st->dtype == QPE_C128 ? 16 : 8;
+  st->N = 1ull << st->P;
+  if (st->ld == 0) throw Error(QPE_ERR_INVALID, "empty block");
+  st->data.alloc(st->N * st->ld * st->esz);
+  st->dk.alloc(sizeof(int));
+  st->probs.alloc(st->N * sizeof(double));
+  // QIFT geometry: T columns per CTA, shared-memory tile N x T.
+  const size_t row_bytes = st->N * st->esz;
+  if (row_bytes > st->ctx->smem_optin) throw Error(QPE_ERR_UNSUPPORTED, "precision too large for the QIFT tile");
+  uint32_t T = 32;
+  while (T > 1 && (row_bytes * T > 96 * 1024 || T > st->ld)) T >>= 1;
+  st->qift_T = T;
+  uint64_t tiles = (st->ld + T - 1) / T;
+  uint64_t grid = (uint64_t)st->ctx->num_sms * 2;
+  if (grid > tiles) grid = tiles;
+  st->qift_grid = (uint32_t)grid;
+  st->partial.alloc(grid * st->N * sizeof(double));
+  // Twiddles exp(-2 pi i k / N), k < N / 2, rounded from long double (as the oracle).
+  const uint64_t nh = st->N / 2 ? st->N / 2 : 1;
+  std::vector<double> twd(2 * nh);
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  for (uint64_t k = 0; k < nh; ++k) {
+    long double ang = -two_pi * (long double)k / (long double)st->N;
+    twd[2 * k] = (double)cosl(ang);
+    twd[2 * k + 1] = (double)sinl(ang);
+  }
+  if (st->dtype == QPE_C128) {
+    st->tw.alloc(twd.size() * sizeof(double));
+    QPE_CK(cudaMemcpy(st->tw.p, twd.data(), twd.size() * sizeof(double), cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> twf(twd.begin(), twd.end());
+    st->tw.alloc(twf.size() * sizeof(float));
+    QPE_CK(cudaMemcpy(st->tw.p, twf.data(), twf.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  const size_t qsm = qift_smem_bytes(st->P, T, st->dtype);
+  QPE_CK(configure_qift_kernels(st->dtype, qsm));
+}
+
+static void build_device_program(qpe_program* pr) {
+  qpe_context* ctx = pr->ctx;
+  HostProgram& hp = pr->hp;
+  cudaStream_t s = ctx->stream;
+  pr->pool.alloc(hp.pool_words * sizeof(uint32_t));
+  pr->ops.alloc(hp.ops.size() * sizeof(DevOp));
+  pr->coef.alloc(hp.coefs.size() * sizeof(double));
+  pr->strA.alloc(hp.Ca * sizeof(uint32_t));
+  pr->strB.alloc(hp.Cb * sizeof(uint32_t));
+  if (!hp.ops.empty())
+    QPE_CK(cudaMemcpyAsync(pr->ops.p, hp.ops.data(), hp.ops.size() * sizeof(DevOp), cudaMemcpyHostToDevice, s));
+  if (!hp.coefs.empty())
+    QPE_CK(cudaMemcpyAsync(pr->coef.p, hp.coefs.data(), hp.coefs.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+  QPE_CK(launch_line_strings(ctx->binom.as<uint64_t>(), hp.M, hp.na, pr->strA.as<uint32_t>(), (uint32_t)hp.Ca, s));
+  QPE_CK(launch_line_strings(ctx->binom.as<uint64_t>(), hp.M, hp.nb, pr->strB.as<uint32_t>(), (uint32_t)hp.Cb, s));
+  // Index tables: one thread per entry.
+  std::vector<uint32_t> start(hp.tables.size() + 1, 0);
+  uint64_t total = 0;
+  for (size_t i = 0; i < hp.tables.size(); ++i) {
+    start[i] = (uint32_t)total;
+    total += hp.tables[i].count;
+  }
+  start[hp.tables.size()] = (uint32_t)total;
+  if (!hp.tables.empty()) {
+    pr->tabs.alloc(hp.tables.size() * sizeof(AxisTable));
+    pr->start.alloc(start.size() * sizeof(uint32_t));
+    QPE_CK(cudaMemcpyAsync(pr->tabs.p, hp.tables.data(), hp.tables.size() * sizeof(AxisTable), cudaMemcpyHostToDevice, s));
+    QPE_CK(cudaMemcpyAsync(pr->start.p, start.data(), start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    QPE_CK(launch_build_tables(ctx->binom.as<uint64_t>(), pr->tabs.as<AxisTable>(), pr->start.as<uint32_t>(),
+                               (uint32_t)hp.tables.size(), total, pr->pool.as<uint32_t>(), s));
+  }
+  QPE_CK(cudaStreamSynchronize(s));
+}
+
+// Launch geometry of one pass for a state of element size esz.
+static PassLaunch plan_pass(const qpe_program* pr, const qpe_state* st, const Pass& pass) {
+  const HostProgram& hp = pr->hp;
+  PassLaunch pl{};
+  pl.work = st->work.p;
+  pl.pool = pr->pool.as<uint32_t>();
+  pl.ops = pr->ops.as<DevOp>();
+  pl.coef = pr->coef.as<double>();
+  pl.strA = pr->strA.as<uint32_t>();
+  pl.strB = pr->strB.as<uint32_t>();
+  pl.Ca = (uint32_t)hp.Ca;
+  pl.Cb = (uint32_t)hp.Cb;
+  pl.pass = pass;
+  pl.exact = st->dtype == QPE_C128 ? 1u : 0u;
+  const size_t esz = st->esz;
+  const size_t warp_budget = 24 * 1024;
+  uint32_t W = 1;
+  if (pass.type == PASS_COL) {
+    while (W < 8 && (size_t)hp.Ca * (W * 2) * esz <= warp_budget && (W * 2) * 2 <= hp.Cb) W *= 2;
+  }
+  pl.W = W;
+  const size_t stage = pass_stage_elems(pass, pl.Ca, pl.Cb, W) * esz;
+  if (stage > st->ctx->smem_optin) throw Error(QPE_ERR_UNSUPPORTED, "block too large for a shared-memory tile");
+  uint32_t wpc = 4;
+  while (wpc > 1 && stage * wpc > st->ctx->smem_optin) --wpc;
+  pl.warps_per_cta = wpc;
+  uint64_t ntiles = pass.type == PASS_COL ? (hp.Cb + W - 1) / W : (pass.type == PASS_ROW ? hp.Ca : pass.mixcount);
+  uint64_t grid = (ntiles + wpc - 1) / wpc;
+  const uint64_t cap = (uint64_t)st->ctx->num_sms * 8;
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  pl.grid = (uint32_t)grid;
+  return pl;
+}
+
+static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts) {
+  const HostProgram& hp = pr->hp;
+  if (hp.M != st->M || hp.na != st->na || hp.nb != st->nb)
+    throw Error(QPE_ERR_INVALID, "program and state shapes differ");
+  uint32_t first = 1, last = (uint32_t)st->N;
+  if (opts && (opts->first_power || opts->last_power)) {
+    first = opts->first_power;
+    last = opts->last_power;
+  }
+  if (first < 1 || last > st->N || first > last) throw Error(QPE_ERR_INVALID, "power range outside 1 .. 2^P");
+  cudaStream_t s = st->ctx->stream;
+  if (!st->work.p) st->work.alloc(st->ld * st->esz);
+  // Working block <- block first - 1.
+  QPE_CK(cudaMemcpyAsync(st->work.p, st->data.as<char>() + (size_t)(first - 1) * st->ld * st->esz,
+                         st->ld * st->esz, cudaMemcpyDeviceToDevice, s));
+  k_set_int<<<1, 1, 0, s>>>(st->dk.as<int>(), (int)first);
+  QPE_CK(cudaGetLastError());
+  st->probs_valid = false;
+  if (first == last) {
+    QPE_CK(cudaStreamSynchronize(s));
+    return;
+  }
+  if (st->graph_prog != pr->id || !st->graph) {
+    if (st->graph) cudaGraphExecDestroy(st->graph);
+    st->graph = nullptr;
+    st->graph_prog = 0;
+    std::vector<PassLaunch> plans;
+    size_t max_smem = 0;
+    for (const Pass& pass : hp.passes) {
+      plans.push_back(plan_pass(pr, st, pass));
+      const PassLaunch& pl = plans.back();
+      size_t sm = pass_stage_elems(pass, pl.Ca, pl.Cb, pl.W) * st->esz * pl.warps_per_cta;
+      if (sm > max_smem) max_smem = sm;
+    }
+    QPE_CK(configure_pass_kernels(st->dtype, max_smem < 48 * 1024 ? 48 * 1024 : max_smem));
+    cudaGraph_t g = nullptr;
+    QPE_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t cap_err = cudaSuccess;
+    for (const PassLaunch& pl : plans)
+      if (cap_err == cudaSuccess) cap_err = launch_pass(pl, st->dtype, s);
+    if (cap_err == cudaSuccess) cap_err = launch_snapshot(st->work.p, st->data.p, st->ld, st->dk.as<int>(), st->dtype, s);
+    if (cap_err == cudaSuccess) cap_err = launch_advance(st->dk.as<int>(), s);
+    cudaError_t end_err = cudaStreamEndCapture(s, &g);
+    if (cap_err != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      QPE_CK(cap_err);
+    }
+    QPE_CK(end_err);
+    cudaGraphExec_t ge = nullptr;
+    cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    QPE_CK(ie);
+    st->graph = ge;
+    st->graph_prog = pr->id;
+  }
+  for (uint32_t k = first; k < last; ++k) QPE_CK(cudaGraphLaunch(st->graph, s));
+  QPE_CK(cudaStreamSynchronize(s));
+}
+
+static void qift(qpe_state* st) {
+  cudaStream_t s = st->ctx->stream;
+  const double norm = std::sqrt((double)st->N);
+  QPE_CK(launch_qift(st->data.p, st->ld, st->P, st->tw.p, norm, st->partial.as<double>(), st->qift_grid, st->qift_T,
+                     st->dtype, s));
+  QPE_CK(launch_reduce_partials(st->partial.as<double>(), st->qift_grid, (uint32_t)st->N, st->probs.as<double>(), s));
+  QPE_CK(cudaStreamSynchronize(s));
+  st->probs_valid = true;
+}
+
+static void check_state(qpe_state* st) {
+  if (!st) throw Error(QPE_ERR_INVALID, "null state");
+  use_device(st->ctx);
+}
+
+static TermArrays term_arrays(const qpe_term* pp, size_t n_pp, const qpe_term* pq, size_t n_pq,
+                              const qpe_term* pqqp, size_t n_pqqp, const qpe_term* pqqr, size_t n_pqqr,
+                              const qpe_term* pqrs, size_t n_pqrs) {
+  TermArrays T{{pp, pq, pqqp, pqqr, pqrs}, {n_pp, n_pq, n_pqqp, n_pqqr, n_pqrs}};
+  for (int i = 0; i < 5; ++i)
+    if (T.n[i] && !T.t[i]) throw Error(QPE_ERR_INVALID, "null term array with nonzero count");
+  return T;
+}
+
+}  // namespace qpe
+
+extern "C" {
+
+int qpe_version(void) { return 1; }
+
+const char* qpe_last_error(void) { return qpe::g_last_error.c_str(); }
+
+int qpe_device_count(int* count) {
+  return guard([&] {
+    if (!count) throw Error(QPE_ERR_INVALID, "null argument");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      n = 0;
+    }
+    *count = n;
+  });
+}
+
+int qpe_context_create(int device, qpe_context** out) {
+  return guard([&] {
+    if (!out) throw Error(QPE_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+      cudaGetLastError();
+      throw Error(QPE_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= n) throw Error(QPE_ERR_INVALID, "device index out of range");
+    auto ctx = new qpe_context();
+    try {
+      ctx->device = device;
+      QPE_CK(cudaSetDevice(device));
+      cudaDeviceProp prop;
+      QPE_CK(cudaGetDeviceProperties(&prop, device));
+      if (prop.major < 10) throw Error(QPE_ERR_UNSUPPORTED, "this library is built for sm_103a (GB300)");
+      ctx->num_sms = prop.multiProcessorCount;
+      ctx->smem_optin = prop.sharedMemPerBlockOptin;
+      QPE_CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+      std::vector<uint64_t> tb(64 * BINOM_K);
+      host_ref_binom_table(tb.data());
+      ctx->binom.alloc(tb.size() * sizeof(uint64_t));
+      QPE_CK(cudaMemcpy(ctx->binom.p, tb.data(), tb.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    } catch (...) {
+      if (ctx->stream) cudaStreamDestroy(ctx->stream);
+      delete ctx;
+      throw;
+    }
+    *out = ctx;
+  });
+}
+
+int qpe_context_destroy(qpe_context* ctx) {
+  if (!ctx) return QPE_OK;
+  cudaSetDevice(ctx->device);
+  for (cudaEvent_t& e : ctx->events)
+    if (e) cudaEventDestroy(e);
+  if (ctx->stream) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+  return QPE_OK;
+}
+
+int qpe_synchronize(qpe_context* ctx) {
+  return guard([&] {
+    check_ctx(ctx);
+    QPE_CK(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int qpe_timer_record(qpe_context* ctx, uint32_t slot) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (slot >= 16) throw Error(QPE_ERR_INVALID, "timer slot must be < 16");
+    if (!ctx->events[slot]) QPE_CK(cudaEventCreate(&ctx->events[slot]));
+    QPE_CK(cudaEventRecord(ctx->events[slot], ctx->stream));
+  });
+}
+
+int qpe_timer_elapsed_ms(qpe_context* ctx, uint32_t a, uint32_t b, float* ms) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (a >= 16 || b >= 16 || !ctx->events[a] || !ctx->events[b] || !ms)
+      throw Error(QPE_ERR_INVALID, "timer slots not recorded");
+    QPE_CK(cudaEventSynchronize(ctx->events[b]));
+    QPE_CK(cudaEventElapsedTime(ms, ctx->events[a], ctx->events[b]));
+  });
+}
+
+int qpe_flush_l2(qpe_context* ctx) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (!ctx->flush.p) ctx->flush.alloc(256ull << 20);
+    QPE_CK(cudaMemsetAsync(ctx->flush.p, 0x5a, ctx->flush.bytes, ctx->stream));
+  });
+}
+
+int qpe_host_alloc(size_t bytes, void** out) {
+  return guard([&] {
+    if (!out) throw Error(QPE_ERR_INVALID, "null output");
+    *out = nullptr;
+    QPE_CK(cudaMallocHost(out, bytes ? bytes : 16));
+  });
+}
+
+int qpe_host_free(void* p) {
+  return guard([&] {
+    if (p) QPE_CK(cudaFreeHost(p));
+  });
+}
+
+int qpe_rank(qpe_context* ctx, const uint64_t* bvs, int64_t* ranks, size_t n) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (n && (!bvs || !ranks)) throw Error(QPE_ERR_INVALID, "null argument");
+    if (!n) return;
+    DevBuf a, b;
+    a.alloc(n * 8);
+    b.alloc(n * 8);
+    QPE_CK(cudaMemcpyAsync(a.p, bvs, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    QPE_CK(launch_rank(ctx->binom.as<uint64_t>(), a.as<uint64_t>(), b.as<int64_t>(), n, ctx->stream));
+    QPE_CK(cudaMemcpyAsync(ranks, b.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    QPE_CK(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int qpe_unrank(qpe_context* ctx, uint32_t nbits, uint32_t weight, const int64_t* ranks, uint64_t* bvs, size_t n) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (n && (!bvs || !ranks)) throw Error(QPE_ERR_INVALID, "null argument");
+    if (nbits == 0 || nbits > 32 || weight > nbits) throw Error(QPE_ERR_INVALID, "need 0 < nbits <= 32, weight <= nbits");
+    const uint64_t total = binom((int)nbits, (int)weight);
+    for (size_t i = 0; i < n; ++i)
+      if (ranks[i] < 0 || (uint64_t)ranks[i] >= total) throw Error(QPE_ERR_INVALID, "rank out of range");
+    if (!n) return;
+    DevBuf a, b;
+    a.alloc(n * 8);
+    b.alloc(n * 8);
+    QPE_CK(cudaMemcpyAsync(a.p, ranks, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    QPE_CK(launch_unrank(ctx->binom.as<uint64_t>(), nbits, weight, a.as<int64_t>(), b.as<uint64_t>(), n, ctx->stream));
+    QPE_CK(cudaMemcpyAsync(bvs, b.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    QPE_CK(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int qpe_rank_with_swaps(qpe_context* ctx, uint32_t nbits, uint64_t bv, const uint32_t* swaps, int64_t* ranks,
+                        size_t nq) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (nq && (!swaps || !ranks)) throw Error(QPE_ERR_INVALID, "null argument");
+    if (nbits == 0 || nbits > 63) throw Error(QPE_ERR_INVALID, "need 0 < nbits <= 63");
+    if (nbits < 64 && (bv >> nbits) != 0) throw Error(QPE_ERR_INVALID, "bit vector wider than nbits");
+    for (size_t i = 0; i < nq; ++i) {
+      const uint32_t* q = swaps + 4 * i;
+      if (q[0] >= nbits || q[1] >= nbits || (q[2] != 0xffffffffu && (q[2] >= nbits || q[3] >= nbits)))
+        throw Error(QPE_ERR_INVALID, "swap position out of range");
+    }
+    if (!nq) return;
+    DevBuf a, b;
+    a.alloc(nq * 16);
+    b.alloc(nq * 8);
+    QPE_CK(cudaMemcpyAsync(a.p, swaps, nq * 16, cudaMemcpyHostToDevice, ctx->stream));
+    QPE_CK(launch_rank_with_swaps(ctx->binom.as<uint64_t>(), nbits, bv, a.as<uint32_t>(), b.as<int64_t>(), nq,
+                                  ctx->stream));
+    QPE_CK(cudaMemcpyAsync(ranks, b.p, nq * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    QPE_CK(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int qpe_axis_table(qpe_context* ctx, int kind, uint32_t nbits, uint32_t weight, const uint32_t* orbitals,
+                   uint32_t* i01, uint32_t* i10, uint8_t* parity, size_t cap, size_t* count) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (!orbitals || !count) throw Error(QPE_ERR_INVALID, "null argument");
+    if (kind < 0 || kind > 4) throw Error(QPE_ERR_INVALID, "unknown table kind");
+    if (nbits == 0 || nbits > 31 || weight > nbits) throw Error(QPE_ERR_INVALID, "need 0 < nbits <= 31, weight <= nbits");
+    static const int nfix[5] = {1, 2, 2, 3, 4}, nocc[5] = {1, 2, 1, 2, 2};
+    AxisTable t{};
+    t.kind = (uint8_t)kind;
+    t.nbits = (uint8_t)nbits;
+    t.weight = (uint8_t)weight;
+    t.nfixed = (uint8_t)nfix[kind];
+    for (int i = 0; i < nfix[kind]; ++i) {
+      if (orbitals[i] >= nbits) throw Error(QPE_ERR_INVALID, "orbital out of range");
+      for (int j = 0; j < i; ++j)
+        if (orbitals[j] == orbitals[i]) throw Error(QPE_ERR_INVALID, "orbitals repeat");
+      t.o[i] = (uint8_t)orbitals[i];
+    }
+    const uint64_t n = binom((int)nbits - nfix[kind], (int)weight - nocc[kind]);
+    *count = (size_t)n;
+    if (n > cap) throw Error(QPE_ERR_INVALID, "output capacity too small");
+    if (n == 0) return;
+    if (n > 0x7fffffffull) throw Error(QPE_ERR_UNSUPPORTED, "table too large");
+    if (!i01 || ((kind == 2 || kind == 3 || kind == 4) && (!i10 || !parity))) throw Error(QPE_ERR_INVALID, "null output");
+    t.count = (uint32_t)n;
+    const bool pairs = kind >= 2;
+    DevBuf tabs, start, pool;
+    tabs.alloc(sizeof(AxisTable));
+    start.alloc(2 * sizeof(uint32_t));
+    pool.alloc(n * (pairs ? 8 : 4));
+    uint32_t st[2] = {0, (uint32_t)n};
+    QPE_CK(cudaMemcpyAsync(tabs.p, &t, sizeof(t), cudaMemcpyHostToDevice, ctx->stream));
+    QPE_CK(cudaMemcpyAsync(start.p, st, sizeof(st), cudaMemcpyHostToDevice, ctx->stream));
+    QPE_CK(launch_build_tables(ctx->binom.as<uint64_t>(), tabs.as<AxisTable>(), start.as<uint32_t>(), 1, n,
+                               pool.as<uint32_t>(), ctx->stream));
+    std::vector<uint32_t> h(n * (pairs ? 2 : 1));
+    QPE_CK(cudaMemcpyAsync(h.data(), pool.p, h.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    QPE_CK(cudaStreamSynchronize(ctx->stream));
+    for (uint64_t j = 0; j < n; ++j) {
+      if (pairs) {
+        i01[j] = h[2 * j] & 0x7fffffffu;
+        parity[j] = (uint8_t)(h[2 * j] >> 31);
+        i10[j] = h[2 * j + 1];
+      } else {
+        i01[j] = h[j];
+        if (parity) parity[j] = 0;
+      }
+    }
+  });
+}
+
+int qpe_program_create(qpe_context* ctx, uint32_t M, uint32_t na, uint32_t nb, const qpe_term* pp, size_t n_pp,
+                       const qpe_term* pq, size_t n_pq, const qpe_term* pqqp, size_t n_pqqp, const qpe_term* pqqr,
+                       size_t n_pqqr, const qpe_term* pqrs, size_t n_pqrs, uint32_t order, uint32_t steps,
+                       qpe_program** out) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (!out) throw Error(QPE_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    TermArrays T = term_arrays(pp, n_pp, pq, n_pq, pqqp, n_pqqp, pqqr, n_pqqr, pqrs, n_pqrs);
+    auto pr = new qpe_program();
+    try {
+      static std::atomic<uint64_t> next_id{1};
+      pr->ctx = ctx;
+      pr->id = next_id++;
+      build_program(pr->hp, M, na, nb, T, order, steps);
+      build_device_program(pr);
+    } catch (...) {
+      delete pr;
+      throw;
+    }
+    *out = pr;
+  });
+}
+
+int qpe_program_destroy(qpe_program* pr) {
+  if (!pr) return QPE_OK;
+  cudaSetDevice(pr->ctx->device);
+  delete pr;
+  return QPE_OK;
+}
+
+static void fill_info(const HostProgram& hp, qpe_program_info* info);
+
+int qpe_program_plan(uint32_t M, uint32_t na, uint32_t nb, const qpe_term* pp, size_t n_pp, const qpe_term* pq,
+                     size_t n_pq, const qpe_term* pqqp, size_t n_pqqp, const qpe_term* pqqr, size_t n_pqqr,
+                     const qpe_term* pqrs, size_t n_pqrs, uint32_t order, uint32_t steps, qpe_program_info* info) {
+  return guard([&] {
+    if (!info) throw Error(QPE_ERR_INVALID, "null output");
+    TermArrays T = term_arrays(pp, n_pp, pq, n_pq, pqqp, n_pqqp, pqqr, n_pqqr, pqrs, n_pqrs);
+    HostProgram hp;
+    build_program(hp, M, na, nb, T, order, steps);
+    fill_info(hp, info);
+  });
+}
+
+int qpe_program_get_info(const qpe_program* pr, qpe_program_info* info) {
+  if (!pr || !info) return fail(QPE_ERR_INVALID, "null argument");
+  fill_info(pr->hp, info);
+  return QPE_OK;
+}
+
+static void fill_info(const HostProgram& hp, qpe_program_info* info) {
+  info->num_orbitals = hp.M;
+  info->n_alpha = hp.na;
+  info->n_beta = hp.nb;
+  info->c_alpha = (uint32_t)hp.Ca;
+  info->c_beta = (uint32_t)hp.Cb;
+  info->num_ops = hp.ops_per_sweep;
+  info->num_ops_per_power = (uint32_t)hp.ops.size();
+  info->touches_per_sweep = hp.touches_per_sweep;
+  info->touches_per_power = hp.touches_per_power;
+  uint64_t entries = 0;
+  for (const AxisTable& t : hp.tables) entries += t.count;
+  info->table_entries = entries;
+  info->num_passes_per_power = (uint32_t)hp.passes.size();
+  info->reserved = 0;
+}
+
+int qpe_state_create(qpe_context* ctx, uint32_t M, uint32_t na, uint32_t nb, uint32_t P, int dtype, qpe_state** out) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (!out) throw Error(QPE_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    if (M == 0 || M > 31 || na == 0 || nb == 0 || na > M || nb > M) throw Error(QPE_ERR_INVALID, "bad shape");
+    if (P == 0 || P > 13) throw Error(QPE_ERR_UNSUPPORTED, "precision must be in 1..13");
+    if (dtype != QPE_C128 && dtype != QPE_C64) throw Error(QPE_ERR_INVALID, "unknown dtype");
+    auto st = new qpe_state();
+    try {
+      st->ctx = ctx;
+      st->M = M;
+      st->na = na;
+      st->nb = nb;
+      st->P = P;
+      st->dtype = dtype;
+      st->Ca = binom((int)M, (int)na);
+      st->Cb = binom((int)M, (int)nb);
+      st->ld = st->Ca * st->Cb;
+      state_alloc(st);
+      QPE_CK(cudaMemsetAsync(st->data.p, 0, st->data.bytes, ctx->stream));
+      QPE_CK(cudaStreamSynchronize(ctx->stream));
+    } catch (...) {
+      delete st;
+      throw;
+    }
+    *out = st;
+  });
+}
+
+int qpe_state_destroy(qpe_state* st) {
+  if (!st) return QPE_OK;
+  cudaSetDevice(st->ctx->device);
+  delete st;
+  return QPE_OK;
+}
+
+int qpe_state_upload(qpe_state* st, const void* host, uint64_t first, uint64_t count) {
+  return guard([&] {
+    check_state(st);
+    if (count && !host) throw Error(QPE_ERR_INVALID, "null host pointer");
+    if (first > st->N * st->ld || count > st->N * st->ld - first) throw Error(QPE_ERR_INVALID, "range outside the state");
+    if (!count) return;
+    QPE_CK(cudaMemcpyAsync(st->data.as<char>() + first * st->esz, host, count * st->esz, cudaMemcpyHostToDevice,
+                           st->ctx->stream));
+    QPE_CK(cudaStreamSynchronize(st->ctx->stream));
+    st->probs_valid = false;
+  });
+}
+
+int qpe_state_download(qpe_state* st, void* host, uint64_t first, uint64_t count) {
+  return guard([&] {
+    check_state(st);
+    if (count && !host) throw Error(QPE_ERR_INVALID, "null host pointer");
+    if (first > st->N * st->ld || count > st->N * st->ld - first) throw Error(QPE_ERR_INVALID, "range outside the state");
+    if (!count) return;
+    QPE_CK(cudaMemcpyAsync(host, st->data.as<char>() + first * st->esz, count * st->esz, cudaMemcpyDeviceToHost,
+                           st->ctx->stream));
+    QPE_CK(cudaStreamSynchronize(st->ctx->stream));
+  });
+}
+
+int qpe_state_zero(qpe_state* st) {
+  return guard([&] {
+    check_state(st);
+    QPE_CK(cudaMemsetAsync(st->data.p, 0, st->data.bytes, st->ctx->stream));
+    QPE_CK(cudaStreamSynchronize(st->ctx->stream));
+    st->probs_valid = false;
+  });
+}
+
+int qpe_evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts) {
+  return guard([&] {
+    check_state(st);
+    if (!pr) throw Error(QPE_ERR_INVALID, "null program");
+    if (opts && opts->strategy != QPE_STRATEGY_AUTO && opts->strategy != QPE_STRATEGY_TILED)
+      throw Error(QPE_ERR_UNSUPPORTED, "strategy not available");
+    evolve(st, pr, opts);
+  });
+}
+
+int qpe_state_qift(qpe_state* st) {
+  return guard([&] {
+    check_state(st);
+    qift(st);
+  });
+}
+
+int qpe_state_phase_probs(qpe_state* st, double* probs) {
+  return guard([&] {
+    check_state(st);
+    if (!probs) throw Error(QPE_ERR_INVALID, "null output");
+    if (!st->probs_valid) {
+      QPE_CK(launch_block_sums(st->data.p, st->ld, (uint32_t)st->N, st->probs.as<double>(), st->dtype, st->ctx->stream));
+    }
+    QPE_CK(cudaMemcpyAsync(probs, st->probs.p, st->N * sizeof(double), cudaMemcpyDeviceToHost, st->ctx->stream));
+    QPE_CK(cudaStreamSynchronize(st->ctx->stream));
+  });
+}
+
+int qpe_state_block_norms(qpe_state* st, double* norms) {
+  return guard([&] {
+    check_state(st);
+    if (!norms) throw Error(QPE_ERR_INVALID, "null output");
+    DevBuf tmp;
+    tmp.alloc(st->N * sizeof(double));
+    QPE_CK(launch_block_sums(st->data.p, st->ld, (uint32_t)st->N, tmp.as<double>(), st->dtype, st->ctx->stream));
+    QPE_CK(cudaMemcpyAsync(norms, tmp.p, st->N * sizeof(double), cudaMemcpyDeviceToHost, st->ctx->stream));
+    QPE_CK(cudaStreamSynchronize(st->ctx->stream));
+  });
+}
+
+// ---- one-shot calls ----
+
+int qpe_time_evolve_over_terms(qpe_context* ctx, uint32_t M, uint32_t e, uint32_t P, const qpe_term* pp, size_t n_pp,
+                               const qpe_term* pq, size_t n_pq, const qpe_term* pqqp, size_t n_pqqp,
+                               const qpe_term* pqqr, size_t n_pqqr, const qpe_term* pqrs, size_t n_pqrs,
+                               double* state) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (!state) throw Error(QPE_ERR_INVALID, "null state");
+    qpe_program* pr = nullptr;
+    qpe_state* st = nullptr;
+    int rc = qpe_program_create(ctx, M, e, e, pp, n_pp, pq, n_pq, pqqp, n_pqqp, pqqr, n_pqqr, pqrs, n_pqrs, 1, 1, &pr);
+    if (rc) throw Error(rc, g_last_error);
+    rc = qpe_state_create(ctx, M, e, e, P, QPE_C128, &st);
+    if (rc) {
+      qpe_program_destroy(pr);
+      throw Error(rc, g_last_error);
+    }
+    const uint64_t ld = st->ld, total = st->N * ld;
+    rc = qpe_state_upload(st, state, 0, ld);
+    if (!rc) rc = qpe_evolve(st, pr, nullptr);
+    if (!rc) rc = qpe_state_download(st, state, 0, total);
+    std::string msg = g_last_error;
+    qpe_state_destroy(st);
+    qpe_program_destroy(pr);
+    if (rc) throw Error(rc, msg);
+  });
+}
+
+static qpe_state* raw_state(qpe_context* ctx, uint32_t P, uint64_t ld) {
+  if (P == 0 || P > 13) throw Error(QPE_ERR_UNSUPPORTED, "precision must be in 1..13");
+  if (ld == 0) throw Error(QPE_ERR_INVALID, "ld must be positive");
+  auto st = new qpe_state();
+  try {
+    st->ctx = ctx;
+    st->P = P;
+    st->dtype = QPE_C128;
+    st->ld = ld;
+    state_alloc(st);
+  } catch (...) {
+    delete st;
+    throw;
+  }
+  return st;
+}
+
+int qpe_qift(qpe_context* ctx, uint32_t P, uint64_t ld, double* state) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (!state) throw Error(QPE_ERR_INVALID, "null state");
+    qpe_state* st = raw_state(ctx, P, ld);
+    try {
+      const size_t bytes = st->N * ld * 16;
+      QPE_CK(cudaMemcpyAsync(st->data.p, state, bytes, cudaMemcpyHostToDevice, ctx->stream));
+      qift(st);
+      QPE_CK(cudaMemcpyAsync(state, st->data.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+      QPE_CK(cudaStreamSynchronize(ctx->stream));
+    } catch (...) {
+      delete st;
+      throw;
+    }
+    delete st;
+  });
+}
+
+int qpe_identify_phase_amplitudes(qpe_context* ctx, uint32_t P, uint64_t ld, const double* state, double* probs) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (!state || !probs) throw Error(QPE_ERR_INVALID, "null argument");
+    qpe_state* st = raw_state(ctx, P, ld);
+    try {
+      QPE_CK(cudaMemcpyAsync(st->data.p, state, st->N * ld * 16, cudaMemcpyHostToDevice, ctx->stream));
+      QPE_CK(launch_block_sums(st->data.p, ld, (uint32_t)st->N, st->probs.as<double>(), QPE_C128, ctx->stream));
+      QPE_CK(cudaMemcpyAsync(probs, st->probs.p, st->N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      QPE_CK(cudaStreamSynchronize(ctx->stream));
+    } catch (...) {
+      delete st;
+      throw;
+    }
+    delete st;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+// kernels.h - launch wrappers of the device kernels (kernels.cu, evolve.cu, qift.cu).
+#ifndef QPE_KERNELS_H_
+#define QPE_KERNELS_H_
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/qpe_gb300.h"
+#include "program.h"
+
+namespace qpe {
+
+// Binomial table with the reference nChoosek's values (cpp/util.hpp:49-60):
+// BINOM_K columns per row, rows n = 0..63.
+constexpr int BINOM_K = 65;
+void host_ref_binom_table(uint64_t* out /* 64 * BINOM_K */);
+
+cudaError_t launch_rank(const uint64_t* d_binom, const uint64_t* bvs, int64_t* ranks, size_t n, cudaStream_t s);
+cudaError_t launch_unrank(const uint64_t* d_binom, uint32_t nbits, uint32_t weight, const int64_t* ranks,
+                          uint64_t* bvs, size_t n, cudaStream_t s);
+cudaError_t launch_rank_with_swaps(const uint64_t* d_binom, uint32_t nbits, uint64_t bv, const uint32_t* swaps,
+                                   int64_t* out, size_t nq, cudaStream_t s);
+// Strings of rank 0..count-1 (weight `weight` over `nbits` bits).
+cudaError_t launch_line_strings(const uint64_t* d_binom, uint32_t nbits, uint32_t weight, uint32_t* out,
+                                uint32_t count, cudaStream_t s);
+cudaError_t launch_build_tables(const uint64_t* d_binom, const AxisTable* d_tabs, const uint32_t* d_entry_start,
+                                uint32_t ntabs, uint64_t total_entries, uint32_t* d_pool, cudaStream_t s);
+
+// ---- evolution (evolve.cu) ----
+struct PassLaunch {
+  void* work;                 // working block (Ca x Cb complex)
+  const uint32_t* pool;
+  const DevOp* ops;
+  const double* coef;
+  const uint32_t* strA;       // alpha strings by rank
+  const uint32_t* strB;       // beta strings by rank
+  uint32_t Ca, Cb;
+  Pass pass;
+  uint32_t W;                 // COL pass: lines per tile (power of two)
+  uint32_t warps_per_cta;
+  uint32_t grid;
+  uint32_t exact;             // complex128: reference rounding (no contraction)
+};
+size_t pass_stage_elems(const Pass& pass, uint32_t Ca, uint32_t Cb, uint32_t W);
+cudaError_t launch_pass(const PassLaunch& pl, int dtype, cudaStream_t s);
+cudaError_t launch_snapshot(const void* work, void* state, uint64_t block_elems, const int* d_k, int dtype,
+                            cudaStream_t s);
+cudaError_t launch_advance(int* d_k, cudaStream_t s);
+cudaError_t configure_pass_kernels(int dtype, size_t smem_bytes);
+
+// ---- QIFT and reductions (qift.cu) ----
+cudaError_t launch_qift(void* state, uint64_t ld, uint32_t P, const void* twiddles, double norm, double* partial,
+                        uint32_t grid, uint32_t cols_per_cta, int dtype, cudaStream_t s);
+size_t qift_smem_bytes(uint32_t P, uint32_t cols_per_cta, int dtype);
+cudaError_t configure_qift_kernels(int dtype, size_t smem_bytes);
+cudaError_t launch_reduce_partials(const double* partial, uint32_t nparts, uint32_t N, double* out, cudaStream_t s);
+cudaError_t launch_block_sums(const void* state, uint64_t ld, uint32_t N, double* out, int dtype, cudaStream_t s);
+
+}  // namespace qpe
+
+#endif  // QPE_KERNELS_H_

@@ -1,0 +1,343 @@
+"""Benchmark of the QPE hot path on GB300.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+
+One step is one full QPE run of the workload: the controlled evolution of all
+2^P - 1 powers, the QIFT and the phase histogram. The metric is amplitude-term
+updates per second (a pair update counts 2, a diagonal phase 1, the same
+definition for every arm). `value` is timed with CUDA events on the library's
+stream with the register resident in HBM; `e2e` repeats the step through host
+buffers (block 0 copied in from page-locked memory, the whole register and the
+histogram copied back) inside the timed region. L2 is flushed between steps.
+
+--impl reference runs the CPU restatement of the reference (oracle/, all host
+threads) on a bounded sample of the same workload and prints its own line.
+Under torchrun (N > 1) every rank runs an independent replica (the path does not
+shard); rank 0 prints, with the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+import __graft_entry__ as graft  # noqa: E402
+
+FP64_PEAK_TFLOPS = 1.19  # measured FP64 FMA throughput of this GB300 (own probe; not in MEASURED_PEAKS.json)
+
+WORKLOADS = {
+    # BASELINE configs[1]: plain QPE in FP64.
+    "plain-n16": dict(n=16, N=8, P=10, dt=0.05, order=2, steps=4, dtype="c128", seed=0,
+                      desc="Plain QPE, FP64: n=16 spin-orbitals, N=8, 10 ancilla qubits, complex128, 2nd-order "
+                           "Trotter dt=0.05, 4 steps per power, Hartree-Fock start"),
+    # The reference's own CPU-runnable case (BASELINE configs[0]), a parity case.
+    "plain-n8": dict(n=8, N=4, P=6, dt=0.1, order=1, steps=1, dtype="c128", seed=0,
+                     desc="Plain QPE, FP64: n=8, N=4, 6 ancilla qubits, 1st-order Trotter dt=0.1"),
+}
+DEFAULT_WORKLOAD = "plain-n16"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", os.environ.get("LOCAL_RANK", "0"), "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": float(rows[0][2]) if rows else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def setup_dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, ws, local
+    return 0, 1, 0
+
+
+def reduce_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def build_problem(q, w, seed_offset=0):
+    ints = q.synthetic_integrals(w["n"], w["seed"] + seed_offset)
+    # A second-order step applies two half steps: coefficients at dt / 2.
+    t = w["dt"] / 2 if w["order"] == 2 else w["dt"]
+    h = q.Hamiltonian.from_integrals(ints, w["N"] // 2, t)
+    return h, h.segmented_terms()
+
+
+def cpu_baseline(q, w, seg, budget_s=15.0, fast=True):
+    """The oracle (CPU restatement of the reference) on a bounded sample: as many
+    controlled powers as fit in about budget_s, with the better of 1 thread and
+    all host threads. Returns (touches/s, threads, sample description)."""
+    O = graft.load_oracle()
+    orc = O.Oracle(fast=fast)
+    M, e, P = w["n"] // 2, w["N"] // 2, w["P"]
+    C2 = math.comb(M, e) ** 2
+    prog_touches = q.plan_program(seg, M, e, e, w["order"], w["steps"])["touches_per_power"]
+    state = np.zeros((1 << P) * C2, np.complex128)
+    state[0] = 2 ** (-P / 2)
+    ncpu = os.cpu_count() or 1
+    best = None
+    for threads in sorted({1, ncpu}):
+        orc.set_threads(threads)
+        t0 = time.perf_counter()
+        orc.time_evolve(M, e, e, P, seg, state, order=w["order"], steps=w["steps"], first=1, last=2)
+        dt1 = time.perf_counter() - t0
+        if best is None or dt1 < best[1]:
+            best = (threads, dt1)
+    threads, per_power = best
+    orc.set_threads(threads)
+    npow = int(max(1, min((1 << P) - 1, budget_s / max(per_power, 1e-9))))
+    t0 = time.perf_counter()
+    orc.time_evolve(M, e, e, P, seg, state, order=w["order"], steps=w["steps"], first=1, last=1 + npow)
+    el = time.perf_counter() - t0
+    rate = prog_touches * npow / el
+    return rate, threads, (f"{npow} of {(1 << P) - 1} controlled powers of the same workload "
+                           f"({el:.1f} s, {threads} thread(s)); QIFT excluded")
+
+
+def run_ours(args, w, rank, ws, local):
+    q = graft.load_package()
+    N = q._native
+    h, seg = build_problem(q, w, seed_offset=rank)
+    M, e, P = w["n"] // 2, w["N"] // 2, w["P"]
+    dtype = np.complex128 if w["dtype"] == "c128" else np.complex64
+    prog = q.Program(seg, M, e, e, trotter_order=w["order"], steps=w["steps"], device=local)
+    st = q.DeviceState(M, e, e, P, dtype=dtype, device=local)
+    npow = (1 << P) - 1
+    touches_step = prog.touches_per_power * npow
+    block0 = q.hf_block0(st.c_alpha, st.c_beta, P, dtype)
+    ctx = N.context(local)
+    timer = N.Timer(local)
+    lib = N.lib()
+
+    def step():
+        st.evolve(prog)
+        st.qift()
+        return st.phase_probs()
+
+    st.upload(block0)
+    for _ in range(args.warmup):
+        st.upload(block0)
+        step()
+    barrier(ws)
+    clocks = Clocks()
+    clocks.start()
+    total_ms, evolve_ms = 0.0, 0.0
+    for _ in range(args.steps):
+        st.upload(block0)
+        N.check(lib.qpe_flush_l2(ctx))
+        timer.record(0)
+        st.evolve(prog)
+        timer.record(1)
+        st.qift()
+        probs = st.phase_probs()
+        timer.record(2)
+        total_ms += timer.elapsed_ms(0, 2)
+        evolve_ms += timer.elapsed_ms(0, 1)
+    clk = clocks.stop()
+    total_ms = reduce_max(total_ms, ws)
+    barrier(ws)
+
+    # End to end through host buffers: block 0 in from page-locked memory, the
+    # whole register and the histogram back.
+    pin_in = N.PinnedBuffer(st.ld, dtype)
+    pin_in.array[:] = block0
+    pin_out = N.PinnedBuffer(st.size, dtype)
+    probs_host = np.zeros(1 << P)
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        N.check(lib.qpe_flush_l2(ctx))
+        timer.record(3)
+        st.upload(pin_in.array)
+        st.evolve(prog)
+        st.qift()
+        probs_host[:] = st.phase_probs()
+        st.download(out=pin_out.array)
+        timer.record(4)
+        e2e_ms += timer.elapsed_ms(3, 4)
+    e2e_ms = reduce_max(e2e_ms, ws)
+
+    ms_step = total_ms / args.steps
+    value = touches_step * ws / (ms_step / 1e3)
+    e2e_value = touches_step * ws / (e2e_ms / args.steps / 1e3)
+    # Roofline of the dominant kernel family (the tile-pass kernels of the
+    # evolution): algorithmic bytes 2 * sizeof(amplitude) per update.
+    bpt = 32 if w["dtype"] == "c128" else 16
+    ev_s = evolve_ms / args.steps / 1e3
+    achieved = touches_step * bpt / ev_s / 1e9
+    peak, peak_kind = peaks()
+    info = prog.info
+    launches = args.steps * (npow * (info["num_passes_per_power"] + 2) + 1 + 2 + 1)
+    line = {
+        "metric": "amplitude-term updates/s per Trotter step",
+        "value": value,
+        "unit": "touches/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if w["dtype"] == "c128" else "f32",
+        "data": "synthetic: seeded integrals (h_pq ~ N(0,1) exp(-|p-q|/2), (pq|rs) ~ N(0,0.1^2) "
+                "exp(-(|p-q|+|r-s|)/3)), one replica per rank",
+        "config": {"workload": args.workload, "description": w["desc"], "n_spin_orbitals": w["n"],
+                   "electrons": w["N"], "precision": P, "dt": w["dt"], "trotter_order": w["order"],
+                   "steps_per_power": w["steps"], "state": w["dtype"], "amps_per_block": st.ld,
+                   "blocks": 1 << P, "touches_per_power": prog.touches_per_power,
+                   "touches_per_step": touches_step, "l2": "flushed before every timed step",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "kernel": "k_pass (evolution tile passes)",
+                     "fp64": {"achieved_tflops": touches_step * 6 / ev_s / 1e12, "peak_tflops": FP64_PEAK_TFLOPS,
+                              "frac": touches_step * 6 / ev_s / 1e12 / FP64_PEAK_TFLOPS,
+                              "flops_per_touch": 6}} if w["dtype"] == "c128" else
+                    {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_kind, "kernel": "k_pass (evolution tile passes)"},
+        "e2e": {"value": e2e_value, "unit": "touches/s",
+                "h2d_bytes_per_step": int(st.ld * dtype().itemsize),
+                "d2h_bytes_per_step": int(st.size * dtype().itemsize + (1 << P) * 8)},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, threads, sample = cpu_baseline(q, w, seg)
+        line["cpu_baseline"] = {"value": rate, "unit": "touches/s", "cores": threads, "kind": "port",
+                                "sample": sample}
+    return line
+
+
+def run_reference(args, w, rank, ws):
+    if rank != 0:
+        return None
+    q = graft.load_package()
+    h, seg = build_problem(q, w)
+    rates = []
+    sample = ""
+    threads = 1
+    for _ in range(args.warmup and 1):
+        cpu_baseline(q, w, seg, budget_s=2.0)
+    for _ in range(args.steps):
+        r, threads, sample = cpu_baseline(q, w, seg, budget_s=max(5.0, 60.0 / max(args.steps, 1)))
+        rates.append(r)
+    value = statistics.median(rates)
+    M, e, P = w["n"] // 2, w["N"] // 2, w["P"]
+    touches_step = q.plan_program(seg, M, e, e, w["order"], w["steps"])["touches_per_power"] * ((1 << P) - 1)
+    return {"metric": "amplitude-term updates/s per Trotter step", "value": value, "unit": "touches/s",
+            "impl": "reference", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": touches_step / value * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (same integrals as the GPU arm)",
+            "config": {"workload": args.workload, "description": w["desc"]},
+            "cpu_baseline": {"value": value, "unit": "touches/s", "cores": threads, "kind": "port",
+                             "sample": sample + "; CPU restatement of the reference (oracle/qpe_oracle.cc): "
+                                                "the reference's sources are not on this host"},
+            "e2e": {"value": value, "unit": "touches/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    rank, ws, local = setup_dist() if args.impl == "ours" else (int(os.environ.get("RANK", "0")),
+                                                                 int(os.environ.get("WORLD_SIZE", "1")), 0)
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        line = run_reference(args, w, rank, ws)
+    else:
+        line = run_ours(args, w, rank, ws, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if ws > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,213 @@
+/*
+ * qpe_gb300.h - C ABI of the GB300 (sm_103a) implementation of qpe-sim's hot path:
+ * the controlled, Trotterized time evolution of a fixed-electron-count state vector
+ * followed by the batched inverse QFT over the ancilla axis.
+ *
+ * Every entry point returns an int status (QPE_OK == 0). No C++ exception crosses
+ * this boundary; qpe_last_error() returns a thread-local message for the last
+ * failing call on the calling thread.
+ *
+ * State layout (identical to the reference StateVector, cpp/state_vector.hpp:20-42):
+ *   amplitude(k, a, b) at index k * Ca * Cb + a * Cb + b,
+ *   k in [0, 2^P) the ancilla value, a = OffsetComputer::rank of the alpha string,
+ *   b = rank of the beta string, Ca = C(M, Na), Cb = C(M, Nb).
+ *   Host buffers are interleaved (re, im) doubles (std::complex<double>) or floats.
+ * Spin-orbital indices follow SpinIndex::HalfUp (cpp/types.hpp:50-55):
+ *   alpha orbital o -> o, beta orbital o -> M + o (0-based).
+ */
+#ifndef QPE_GB300_H_
+#define QPE_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define QPE_OK 0
+#define QPE_ERR_INVALID 1     /* bad shape, index or argument */
+#define QPE_ERR_UNSUPPORTED 2 /* shape outside what the library handles */
+#define QPE_ERR_NOMEM 3       /* device or host allocation failed */
+#define QPE_ERR_CUDA 4        /* a CUDA runtime call failed */
+#define QPE_ERR_TIMEOUT 5     /* a bounded device-side wait gave up */
+#define QPE_ERR_NO_DEVICE 6   /* no usable CUDA device */
+
+/* ---- state element types ------------------------------------------------ */
+#define QPE_C128 0 /* complex double: the reference's std::complex<double> */
+#define QPE_C64 1  /* complex float state, FP64 coefficients and reductions */
+
+/* ---- term kinds (the five segments of
+ *      Hamiltonian::PrintIndexedSegmentedHamiltonianTerms, cpp/hamiltonian.cc:253-299) */
+#define QPE_TERM_PP 0
+#define QPE_TERM_PQ 1
+#define QPE_TERM_PQQP 2
+#define QPE_TERM_PQQR 3
+#define QPE_TERM_PQRS 4
+
+/*
+ * One indexed Hamiltonian term with its host-computed exponentiated coefficients.
+ *   pp   : key (p, p)        coefficient Hamiltonian::pp_term(p)        -> even[0..1]
+ *   pq   : key (p, q), p > q  pq_term(p, q, parity)                       -> even / odd
+ *   pqqp : key (p, q, q, p)   pqqp_term(p, q)                             -> even[0..1]
+ *   pqqr : key (p, q, q, r)   pqqr_term(p, q, r, parity)                  -> even / odd
+ *   pqrs : key (p, q, r, s)   pqrs_term(p, q, r, s, parity)               -> even / odd
+ * even/odd hold {m00.re, m00.im, m01.re, m01.im} of the symmetric 2x2 matrix
+ * [[m00, m01], [m01, m00]] for JW parity 0 / 1 (cpp/hamiltonian.cc:674-783).
+ * Diagonal terms use even[0], even[1] only. Unused indices are ignored.
+ */
+typedef struct qpe_term {
+  uint32_t p, q, r, s;
+  double even[4];
+  double odd[4];
+} qpe_term;
+
+/* ---- context -------------------------------------------------------------- */
+typedef struct qpe_context qpe_context;
+
+int qpe_version(void);
+const char* qpe_last_error(void);
+int qpe_device_count(int* count);
+int qpe_context_create(int device, qpe_context** out);
+int qpe_context_destroy(qpe_context* ctx);
+int qpe_synchronize(qpe_context* ctx);
+
+/* CUDA events on the context's stream (slots 0..15), for timing the library's
+ * own work on the stream it launches on. */
+int qpe_timer_record(qpe_context* ctx, uint32_t slot);
+int qpe_timer_elapsed_ms(qpe_context* ctx, uint32_t start_slot, uint32_t end_slot, float* ms);
+
+/* Page-locked host memory (cudaMallocHost), for host buffers the copies of
+ * the one-shot and resident APIs read and write at full speed. */
+int qpe_host_alloc(size_t bytes, void** out);
+int qpe_host_free(void* p);
+
+/* Writes a 256 MiB device buffer (allocated on first use) so that the next
+ * timed region starts with nothing of the state in L2. */
+int qpe_flush_l2(qpe_context* ctx);
+
+/* ---- combinatorial primitives (device kernels) ------------------------------ */
+
+/* Replaces OffsetComputer::rank (cpp/offset_computer.hpp:16-27): colex rank
+ * sum_i C(pos_i, i + 1) over the set bits of each bit vector. Host arrays. */
+int qpe_rank(qpe_context* ctx, const uint64_t* bvs, int64_t* ranks, size_t n);
+
+/* Inverse of qpe_rank over the weight-`weight` strings of `nbits` bits (the
+ * enumeration order of next_comb, cpp/util.hpp:62-70). Host arrays. */
+int qpe_unrank(qpe_context* ctx, uint32_t nbits, uint32_t weight, const int64_t* ranks,
+               uint64_t* bvs, size_t n);
+
+/* Replaces OffsetComputer(n, bv, rank).rank_with_swap(i, j) and
+ * .rank_with_double_swap(i, j, k, l) (cpp/offset_computer.hpp:128-192) for a
+ * batch of queries against one bit vector; computed on the device from prefix
+ * tables. `swaps` holds n_queries rows of 4 positions; for a single swap set
+ * the last two to 0xFFFFFFFF. */
+int qpe_rank_with_swaps(qpe_context* ctx, uint32_t nbits, uint64_t bv, const uint32_t* swaps,
+                        int64_t* ranks, size_t n_queries);
+
+/* Replaces the discover*_BVs routines (cpp/time_evolution_over_terms.hpp:1160-1411)
+ * for one term on one spin: builds the index table on the device and returns it
+ * with the runs expanded, entry j being the j-th string of the reference's run
+ * order. kind: 0 N(q), 1 NN(p, r), 2 CA(p, r), 3 CNA(p, q, r), 4 CCAA(p, q, r, s);
+ * orbitals holds those orbitals in that order (0-based within the spin). For the
+ * list kinds (N, NN) i10 is left untouched and parity is 0. *count receives the
+ * number of entries; cap bounds the output arrays. */
+int qpe_axis_table(qpe_context* ctx, int kind, uint32_t nbits, uint32_t weight, const uint32_t* orbitals,
+                   uint32_t* i01, uint32_t* i10, uint8_t* parity, size_t cap, size_t* count);
+
+/* ---- one-shot calls shaped like the reference's (host buffers) -------------- */
+
+/* Replaces time_evolve_over_terms(StateVector&, Hamiltonian&, unsigned precision)
+ * (cpp/time_evolution_over_terms.hpp:92-139). The five arrays are the segmented
+ * indexed terms in map order with their coefficients; the library applies them in
+ * the order of applyUnitary_reordered (:374-562), including the nesting of pqqr
+ * terms under their pq term and the skipping rule of :465. `state` holds
+ * 2^precision * C(M, num_occupied)^2 interleaved complex doubles with block 0
+ * filled; on return every block k holds U^k * block 0. */
+int qpe_time_evolve_over_terms(qpe_context* ctx, uint32_t num_orbitals, uint32_t num_occupied,
+                               uint32_t precision, const qpe_term* pp, size_t n_pp,
+                               const qpe_term* pq, size_t n_pq, const qpe_term* pqqp,
+                               size_t n_pqqp, const qpe_term* pqqr, size_t n_pqqr,
+                               const qpe_term* pqrs, size_t n_pqrs, double* state);
+
+/* Replaces StateVector::qift() (cpp/state_vector.hpp:115-179): in-place forward
+ * DFT (sign -1) of length 2^precision along the ancilla axis (stride ld, ld
+ * transforms), then division by sqrt(2^precision). */
+int qpe_qift(qpe_context* ctx, uint32_t precision, uint64_t ld, double* state);
+
+/* Replaces StateVector::IdentifyPhaseAmplitudes() (cpp/state_vector.hpp:341-372):
+ * probs[k] = sum over the block of |amplitude(k, .)|^2. */
+int qpe_identify_phase_amplitudes(qpe_context* ctx, uint32_t precision, uint64_t ld,
+                                  const double* state, double* probs);
+
+/* ---- device-resident API --------------------------------------------------- */
+
+typedef struct qpe_program qpe_program; /* compiled term program of one Hamiltonian */
+typedef struct qpe_state qpe_state;     /* device-resident 2^P x Ca x Cb state */
+
+typedef struct qpe_program_info {
+  uint32_t num_orbitals, n_alpha, n_beta;
+  uint32_t c_alpha, c_beta;
+  uint32_t num_ops;          /* term applications in one Trotter sweep */
+  uint32_t num_ops_per_power;
+  uint64_t touches_per_sweep; /* amplitude-term updates in one sweep (pair = 2, diagonal = 1) */
+  uint64_t touches_per_power;
+  uint64_t table_entries;     /* device index-table entries */
+  uint32_t num_passes_per_power; /* tile passes (kernel launches) per controlled power */
+  uint32_t reserved;
+} qpe_program_info;
+
+/* Builds the application order and the device pair tables for one Hamiltonian.
+ * n_alpha == n_beta reproduces the reference; n_alpha != n_beta is an extension
+ * (odd electron counts) the reference cannot represent.
+ * trotter_order 1 = the reference's first-order sweep; 2 = symmetric (Strang)
+ * product of a forward and a reversed sweep, each with the coefficients given
+ * (compute them at half the step). steps_per_power repeats the step. */
+int qpe_program_create(qpe_context* ctx, uint32_t num_orbitals, uint32_t n_alpha,
+                       uint32_t n_beta, const qpe_term* pp, size_t n_pp, const qpe_term* pq,
+                       size_t n_pq, const qpe_term* pqqp, size_t n_pqqp, const qpe_term* pqqr,
+                       size_t n_pqqr, const qpe_term* pqrs, size_t n_pqrs, uint32_t trotter_order,
+                       uint32_t steps_per_power, qpe_program** out);
+int qpe_program_destroy(qpe_program* prog);
+/* Host-only planning of the same program (no device work): fills *info. */
+int qpe_program_plan(uint32_t num_orbitals, uint32_t n_alpha, uint32_t n_beta, const qpe_term* pp, size_t n_pp,
+                     const qpe_term* pq, size_t n_pq, const qpe_term* pqqp, size_t n_pqqp, const qpe_term* pqqr,
+                     size_t n_pqqr, const qpe_term* pqrs, size_t n_pqrs, uint32_t trotter_order,
+                     uint32_t steps_per_power, qpe_program_info* info);
+int qpe_program_get_info(const qpe_program* prog, qpe_program_info* info);
+
+int qpe_state_create(qpe_context* ctx, uint32_t num_orbitals, uint32_t n_alpha, uint32_t n_beta,
+                     uint32_t precision, int dtype, qpe_state** out);
+int qpe_state_destroy(qpe_state* st);
+/* Host <-> device copies of elements [first, first + count) of the state, in the
+ * state's element type (interleaved doubles for QPE_C128, floats for QPE_C64). */
+int qpe_state_upload(qpe_state* st, const void* host, uint64_t first, uint64_t count);
+int qpe_state_download(qpe_state* st, void* host, uint64_t first, uint64_t count);
+int qpe_state_zero(qpe_state* st);
+
+#define QPE_STRATEGY_AUTO 0
+#define QPE_STRATEGY_RESIDENT 1 /* whole block in one CTA's shared memory */
+#define QPE_STRATEGY_CLUSTER 2  /* block spread over a thread-block cluster */
+#define QPE_STRATEGY_TILED 3    /* L2-resident block, shared-memory tile passes */
+
+typedef struct qpe_evolve_opts {
+  uint32_t strategy;     /* QPE_STRATEGY_* */
+  uint32_t first_power;  /* evolve blocks first_power .. last_power - 1 (0, 0 = all) */
+  uint32_t last_power;
+  uint32_t cluster_size; /* QPE_STRATEGY_CLUSTER: CTAs per cluster (0 = auto) */
+} qpe_evolve_opts;
+
+/* block_k <- U * block_{k-1} for k = 1 .. 2^P - 1 on the device (opts may be NULL). */
+int qpe_evolve(qpe_state* st, const qpe_program* prog, const qpe_evolve_opts* opts);
+/* In-place QIFT of the device state; also records the phase histogram. */
+int qpe_state_qift(qpe_state* st);
+/* Phase histogram (2^P doubles) of the device state, computed in FP64. */
+int qpe_state_phase_probs(qpe_state* st, double* probs);
+/* Per-block squared norms (2^P doubles, FP64 accumulation). */
+int qpe_state_block_norms(qpe_state* st, double* norms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QPE_GB300_H_ */

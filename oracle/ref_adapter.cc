@@ -1,0 +1,299 @@
+// ref_adapter.cc - C ABI over the reference's own code, compiled from the
+// reference sources where they lie (see oracle/Makefile) into oracle/_ref/.
+// TEST INFRASTRUCTURE ONLY: it produces the golden vectors under tests/golden/
+// and checks the oracle restatement against the reference itself.
+//
+// The reference headers are included unmodified. Hamiltonian keeps the orbital
+// count and identity private (cpp/hamiltonian.hpp:144-150) and only sets them in
+// IngestBroombridge; to build Hamiltonians from synthetic integrals this file opens
+// the class's members for itself by redefining `private` around the include.
+#include <algorithm>
+#include <array>
+#include <cassert>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <iostream>
+#include <map>
+#include <numeric>
+#include <random>
+#include <regex>
+#include <set>
+#include <sstream>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#define private public
+#define protected public
+#include "hamiltonian.hpp"
+#include "offset_computer.hpp"
+#include "state_vector.hpp"
+#include "time_evolution_over_terms.hpp"
+#undef private
+#undef protected
+
+#include "../include/qpe_gb300.h"
+
+double rdouble = 0.0;
+
+namespace {
+
+// Silences the reference's progress printing while a call runs.
+struct Quiet {
+  std::streambuf* old;
+  std::ostringstream sink;
+  Quiet() : old(std::cout.rdbuf(sink.rdbuf())) {}
+  ~Quiet() { std::cout.rdbuf(old); }
+};
+
+void put(const std::array<std::complex<double>, 4>& m, double* d) {
+  d[0] = m[0].real();
+  d[1] = m[0].imag();
+  d[2] = m[1].real();
+  d[3] = m[1].imag();
+}
+
+}  // namespace
+
+extern "C" {
+
+// Hamiltonian from integrals: one_body rows (p, q, v) with 1-based p >= q and
+// two_body rows (p, q, r, s, v) passed to AddTwoBodyTerm as given.
+void* ref_ham_create(unsigned M, unsigned e, double identity, size_t n1, const int* ob_idx, const double* ob_val,
+                     size_t n2, const int* tb_idx, const double* tb_val, double dt) {
+  Quiet q;
+  auto* h = new Hamiltonian();
+  h->max_number_of_orbitals = M;
+  h->num_occupied_ = e;
+  h->identity = identity;
+  for (size_t i = 0; i < n1; ++i) h->AddOneBodyTerm(std::make_pair(ob_idx[2 * i], ob_idx[2 * i + 1]), ob_val[i]);
+  for (size_t i = 0; i < n2; ++i)
+    h->AddTwoBodyTerm(std::make_tuple(tb_idx[4 * i], tb_idx[4 * i + 1], tb_idx[4 * i + 2], tb_idx[4 * i + 3]), tb_val[i]);
+  h->IndexTerms(SpinIndex::HalfUp);
+  h->SetTimestep(dt);
+  return h;
+}
+
+// Hamiltonian::IngestBroombridge on a file; writes block 0 (C^2 amplitudes) into
+// state0 if non-null. Returns 0 or -1 on an exception.
+void* ref_ham_from_broombridge(const char* path, unsigned precision, double dt, unsigned* M, unsigned* e,
+                               double* identity, double* state0, size_t cap) {
+  Quiet q;
+  try {
+    auto* h = new Hamiltonian();
+    StateVector sv = h->IngestBroombridge(path, precision);
+    h->IndexTerms(SpinIndex::HalfUp);
+    h->SetTimestep(dt);
+    *M = h->num_orbitals();
+    *e = h->num_occupied();
+    *identity = h->GetIdentityTerm();
+    if (state0) {
+      size_t n = std::min(cap, sv.size());
+      std::memcpy(state0, sv.data(), n * sizeof(std::complex<double>));
+    }
+    return h;
+  } catch (...) {
+    return nullptr;
+  }
+}
+
+void ref_ham_destroy(void* h) { delete static_cast<Hamiltonian*>(h); }
+
+void ref_ham_set_timestep(void* h, double dt) { static_cast<Hamiltonian*>(h)->SetTimestep(dt); }
+
+void ref_segment_counts(void* hv, size_t* counts) {
+  auto* h = static_cast<Hamiltonian*>(hv);
+  auto seg = h->PrintIndexedSegmentedHamiltonianTerms();
+  counts[0] = std::get<0>(seg).size();
+  counts[1] = std::get<1>(seg).size();
+  counts[2] = std::get<2>(seg).size();
+  counts[3] = std::get<3>(seg).size();
+  counts[4] = std::get<4>(seg).size();
+}
+
+// One segment with the coefficient getters (cpp/hamiltonian.cc:661-783).
+size_t ref_segment_terms(void* hv, int kind, qpe_term* out, double* raw, size_t cap) {
+  auto* h = static_cast<Hamiltonian*>(hv);
+  auto seg = h->PrintIndexedSegmentedHamiltonianTerms();
+  size_t n = 0;
+  auto one = [&](const IdxSingleVec& v) {
+    for (const auto& t : v) {
+      if (n >= cap) break;
+      qpe_term& o = out[n];
+      std::memset(&o, 0, sizeof(o));
+      o.p = t.first.first;
+      o.q = t.first.second;
+      raw[n] = t.second;
+      if (kind == QPE_TERM_PP) {
+        auto c = h->pp_term(o.p);
+        o.even[0] = c.real();
+        o.even[1] = c.imag();
+      } else {
+        put(h->pq_term(o.p, o.q, 0), o.even);
+        put(h->pq_term(o.p, o.q, 1), o.odd);
+      }
+      ++n;
+    }
+  };
+  auto two = [&](const IdxDoubleVec& v) {
+    for (const auto& t : v) {
+      if (n >= cap) break;
+      qpe_term& o = out[n];
+      std::memset(&o, 0, sizeof(o));
+      std::tie(o.p, o.q, o.r, o.s) = t.first;
+      raw[n] = t.second;
+      if (kind == QPE_TERM_PQQP) {
+        auto c = h->pqqp_term(o.p, o.q);
+        o.even[0] = c.real();
+        o.even[1] = c.imag();
+      } else if (kind == QPE_TERM_PQQR) {
+        put(h->pqqr_term(o.p, o.q, o.s, 0), o.even);
+        put(h->pqqr_term(o.p, o.q, o.s, 1), o.odd);
+      } else {
+        put(h->pqrs_term(o.p, o.q, o.r, o.s, 0), o.even);
+        put(h->pqrs_term(o.p, o.q, o.r, o.s, 1), o.odd);
+      }
+      ++n;
+    }
+  };
+  switch (kind) {
+    case QPE_TERM_PP: one(std::get<0>(seg)); break;
+    case QPE_TERM_PQ: one(std::get<1>(seg)); break;
+    case QPE_TERM_PQQP: two(std::get<2>(seg)); break;
+    case QPE_TERM_PQQR: two(std::get<3>(seg)); break;
+    case QPE_TERM_PQRS: two(std::get<4>(seg)); break;
+  }
+  return n;
+}
+
+// time_evolve_over_terms on a StateVector whose block 0 is `state` (C^2 values);
+// the whole 2^P C^2 result is written back to `state`.
+int ref_time_evolve(void* hv, unsigned P, double* state) {
+  Quiet q;
+  auto* h = static_cast<Hamiltonian*>(hv);
+  StateVector sv(P, h->num_orbitals(), h->num_occupied());
+  const uint64_t C = nChoosek(h->num_orbitals(), h->num_occupied());
+  std::memcpy(sv.data(), state, C * C * sizeof(std::complex<double>));
+  time_evolve_over_terms(sv, *h, P);
+  std::memcpy(state, sv.data(), sv.size() * sizeof(std::complex<double>));
+  return 0;
+}
+
+// Seconds per call of applyUnitary_reordered after the setup of
+// time_evolve_over_terms (used to time the reference on a bounded sample).
+double ref_time_steps(void* hv, unsigned P, double* state, unsigned nsteps) {
+  Quiet q;
+  auto* h = static_cast<Hamiltonian*>(hv);
+  StateVector sv(P, h->num_orbitals(), h->num_occupied());
+  const uint64_t C = nChoosek(h->num_orbitals(), h->num_occupied());
+  std::memcpy(sv.data(), state, C * C * sizeof(std::complex<double>));
+  setupGlobals(*h);
+  IdxSingleVec pp, pq;
+  IdxDoubleVec pqqp, pqqr, pqrs;
+  std::tie(pp, pq, pqqp, pqqr, pqrs) = h->PrintIndexedSegmentedHamiltonianTerms();
+  auto t0 = std::chrono::steady_clock::now();
+  for (unsigned k = 1; k <= nsteps && k < (1u << P); ++k) {
+    std::copy_n(sv.begin() + (k - 1) * expbase, expbase, sv.begin() + k * expbase);
+    applyUnitary_reordered(sv, *h, pp, pq, pqqp, pqqr, pqrs, k);
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count() / nsteps;
+}
+
+int ref_qift(unsigned P, unsigned M, unsigned e, double* state) {
+  Quiet q;
+  StateVector sv(P, M, e);
+  std::memcpy(sv.data(), state, sv.size() * sizeof(std::complex<double>));
+  sv.qift();
+  std::memcpy(state, sv.data(), sv.size() * sizeof(std::complex<double>));
+  return 0;
+}
+
+int ref_identify_phase_amplitudes(unsigned P, unsigned M, unsigned e, const double* state, double* probs) {
+  Quiet q;
+  StateVector sv(P, M, e);
+  std::memcpy(sv.data(), state, sv.size() * sizeof(std::complex<double>));
+  auto p = sv.IdentifyPhaseAmplitudes();
+  std::copy(p.begin(), p.end(), probs);
+  return 0;
+}
+
+int64_t ref_rank(uint64_t bv) { return OffsetComputer::rank(bv); }
+
+uint64_t ref_nchoosek(int n, int k) { return nChoosek(n, k); }
+
+int ref_rank_with_swaps(unsigned n, uint64_t bv, const uint32_t* swaps, int64_t* out, size_t nq) {
+  OffsetComputer oc{n, bv, OffsetComputer::rank(bv)};
+  for (size_t i = 0; i < nq; ++i) {
+    const uint32_t* s = swaps + 4 * i;
+    if (s[2] == 0xFFFFFFFFu)
+      out[i] = oc.rank_with_swap(s[0], s[1]);
+    else
+      out[i] = oc.rank_with_double_swap(s[0], s[1], s[2], s[3]);
+  }
+  return 0;
+}
+
+// The discover*_BVs routines (time_evolution_over_terms.hpp:1160-1411), with the
+// vector sized as their callers size it. kind: 0 N, 1 NN, 2 CA, 3 CNA, 4 CCAA.
+int64_t ref_discover(int kind, unsigned M, unsigned e, unsigned p, unsigned q, unsigned r, unsigned s,
+                     uint64_t* niter, uint64_t* off01, uint64_t* off10, unsigned* par, size_t cap) {
+  static const int nfix[5] = {1, 2, 2, 3, 4};
+  static const int nocc[5] = {1, 2, 1, 2, 2};
+  std::vector<MixedPQRSLoopInfo> v(nChoosek((int)M - nfix[kind], (int)e - nocc[kind]));
+  unsigned n = 0;
+  switch (kind) {
+    case 0: n = discoverN_BVs(v, q, e); break;
+    case 1: n = discoverNN_BVs(v, p, r, e); break;
+    case 2: n = discoverCA_BVs(v, p, r, e); break;
+    case 3: n = discoverCNA_BVs(v, p, q, r, e); break;
+    case 4: n = discoverCCAA_BVs(v, p, q, r, s, e); break;
+  }
+  if (n > cap) return -1;
+  for (unsigned i = 0; i < n; ++i) {
+    niter[i] = v[i].niter;
+    off01[i] = v[i].off01;
+    off10[i] = v[i].off10;
+    par[i] = v[i].mid_parity;
+  }
+  return n;
+}
+
+// Runs the reference's embedded doctest cases whose name contains `filter`
+// (empty: all). Writes per-case (checks, failed) pairs; returns the case count.
+int ref_run_doctests(const char* filter, char* names, size_t names_cap, long* checks, long* failed, int cap) {
+#ifdef DOCTEST_CONFIG_DISABLE
+  (void)filter; (void)names; (void)names_cap; (void)checks; (void)failed; (void)cap;
+  return -1;
+#else
+  Quiet q;
+  int n = 0;
+  std::string all;
+  for (const auto& c : doctest_shim::registry()) {
+    if (filter && *filter && std::string(c.name).find(filter) == std::string::npos) continue;
+    if (n >= cap) break;
+    doctest_shim::stats() = doctest_shim::Stats{};
+    bool threw = false;
+    try {
+      c.fn();
+    } catch (const doctest_shim::Abort&) {
+    } catch (...) {
+      threw = true;
+    }
+    checks[n] = doctest_shim::stats().checks;
+    failed[n] = doctest_shim::stats().failed_checks + (threw ? 1 : 0);
+    all += c.name;
+    all += '\n';
+    ++n;
+  }
+  std::strncpy(names, all.c_str(), names_cap - 1);
+  names[names_cap - 1] = 0;
+  return n;
+#endif
+}
+
+}  // extern "C"

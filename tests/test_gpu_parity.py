@@ -1,0 +1,220 @@
+"""GPU path against the oracle (same inputs, this machine) and the golden vectors
+(the reference itself, another machine).
+
+complex128 results are compared bit for bit with the oracle: both use the same
+operation order with every product and sum rounded separately. Against the
+golden vectors (produced on a different CPU) they agree to 1e-13. complex64
+results are compared with the complex128 oracle with the tolerance stated in
+each test.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import evolve_cases, golden_segments, load_golden
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ("pp", "pq", "pqqp", "pqqr", "pqrs")
+
+
+def _seg(q, n, N, seed, dt):
+    return q.Hamiltonian.from_integrals(q.synthetic_integrals(n, seed), N // 2, dt).segmented_terms()
+
+
+def test_rank_and_unrank_against_oracle(gpu, orc):
+    q = gpu
+    rng = np.random.default_rng(1)
+    bvs = rng.integers(0, 1 << 40, size=5000, dtype=np.uint64)
+    bvs[:3] = [0, 1, (1 << 40) - 1]
+    got = q.OffsetComputer.ranks(bvs)
+    assert list(got) == [orc.rank(int(b)) for b in bvs]
+    for nbits, w in [(8, 4), (12, 6), (20, 10), (24, 12), (5, 0), (31, 3), (32, 16)]:
+        total = math.comb(nbits, w)
+        ranks = np.arange(min(total, 20000), dtype=np.int64)
+        s = q.OffsetComputer.unrank(nbits, w, ranks)
+        # colex enumeration order of next_comb, from the smallest string
+        x = (1 << w) - 1
+        for r in range(len(ranks)):
+            assert int(s[r]) == x, (nbits, w, r)
+            x = orc.next_comb(x) if x else 1
+        assert np.array_equal(q.OffsetComputer.ranks(s), ranks)
+
+
+def test_swap_ranks_against_reference(gpu):
+    q = gpu
+    z = load_golden("swaps.npz")
+    qoff = 0
+    for n, bv, cnt in z["heads"]:
+        qs = z["queries"][qoff:qoff + cnt]
+        want = z["ranks"][qoff:qoff + cnt]
+        qoff += cnt
+        oc = q.OffsetComputer(int(n), int(bv))
+        assert np.array_equal(oc.rank_with_swaps(qs), want)
+
+
+def test_device_tables_equal_reference_runs(gpu):
+    """Each device table equals the reference's discover*_BVs runs expanded in
+    order (off01 + i, off10 + i, mid_parity & 1 for i < niter)."""
+    from qpesim_gb300.offset_computer import axis_table
+    z = load_golden("discover.npz")
+    off = 0
+    for kind, M, e, p, q_, r, s, n in z["rows"]:
+        runs = z["tables"][off:off + n]
+        off += n
+        orb = {0: [q_], 1: [p, r], 2: [p, r], 3: [p, q_, r], 4: [p, q_, r, s]}[int(kind)]
+        i01, i10, par = axis_table(int(kind), int(M), int(e), [int(x) for x in orb])
+        w01 = np.concatenate([np.arange(o1, o1 + ni) for ni, o1, _, _ in runs]) if n else np.zeros(0)
+        assert np.array_equal(i01, w01), (kind, M, e, p, q_, r, s)
+        if kind >= 2:
+            w10 = np.concatenate([np.arange(o2, o2 + ni) for ni, _, o2, _ in runs])
+            wp = np.concatenate([np.full(ni, pa & 1) for ni, _, _, pa in runs])
+            assert np.array_equal(i10, w10) and np.array_equal(par, wp), (kind, M, e, p, q_, r, s)
+
+
+@pytest.mark.parametrize("name", evolve_cases())
+def test_golden_evolution_qift_probs(gpu, orc, name):
+    q = gpu
+    z = load_golden(name)
+    n, N, P = int(z["n"]), int(z["N"]), int(z["P"])
+    M, e = n // 2, N // 2
+    seg = golden_segments(z)
+    ld = len(z["block0"])
+    sv = q.StateVector(P, M, e)
+    sv[:ld] = z["block0"]
+    h = q.Hamiltonian.from_integrals(q.synthetic_integrals(n, int(z["seed"])), e, float(z["dt"]))
+    q.time_evolve_over_terms(sv, h, P)
+    ref = np.zeros(len(sv), np.complex128)
+    ref[:ld] = z["block0"]
+    orc.time_evolve(M, e, e, P, seg, ref)
+    assert np.array_equal(np.asarray(sv), ref)
+    np.testing.assert_allclose(np.asarray(sv), z["evolved"], rtol=0, atol=1e-13)
+    sv.qift()
+    orc.qift(P, ld, ref)
+    assert np.array_equal(np.asarray(sv), ref)
+    np.testing.assert_allclose(np.asarray(sv), z["qift"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(sv.IdentifyPhaseAmplitudes(), z["probs"], rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("n,na,nb,P,order,steps", [
+    (8, 2, 2, 5, 1, 1), (12, 3, 3, 3, 1, 1), (14, 4, 3, 2, 1, 1), (10, 1, 1, 3, 1, 1), (10, 5, 5, 2, 1, 1),
+    (10, 2, 3, 3, 2, 3), (12, 2, 2, 2, 2, 1), (16, 4, 4, 2, 1, 1), (6, 3, 3, 3, 1, 1)])
+def test_device_state_against_oracle(gpu, orc, n, na, nb, P, order, steps):
+    q = gpu
+    M = n // 2
+    seg = _seg(q, n, 2 * max(na, nb), 100 + n + na, 0.07)
+    prog = q.Program(seg, M, na, nb, trotter_order=order, steps=steps)
+    st = q.DeviceState(M, na, nb, P)
+    block0 = q.hf_block0(st.c_alpha, st.c_beta, P)
+    rng = np.random.default_rng(n)
+    block0 += (rng.standard_normal(st.ld) + 1j * rng.standard_normal(st.ld)) * 1e-2
+    st.upload(block0)
+    st.evolve(prog)
+    got = st.download()
+    ref = np.zeros(st.size, np.complex128)
+    ref[:st.ld] = block0
+    orc.time_evolve(M, na, nb, P, seg, ref, order=order, steps=steps)
+    assert np.array_equal(got, ref)
+    np.testing.assert_allclose(st.block_norms(), [np.vdot(b, b).real for b in ref.reshape(-1, st.ld)], rtol=1e-12)
+    st.qift()
+    orc.qift(P, st.ld, ref)
+    assert np.array_equal(st.download(), ref)
+    np.testing.assert_allclose(st.phase_probs(), orc.identify_phase_amplitudes(P, st.ld, ref), rtol=1e-12,
+                               atol=1e-16)
+
+
+def test_partial_power_ranges_compose(gpu):
+    q = gpu
+    seg = _seg(q, 10, 6, 9, 0.1)
+    prog = q.Program(seg, 5, 3, 3)
+    a = q.DeviceState(5, 3, 3, 4)
+    b = q.DeviceState(5, 3, 3, 4)
+    b0 = q.hf_block0(a.c_alpha, a.c_beta, 4)
+    a.upload(b0)
+    b.upload(b0)
+    a.evolve(prog)
+    b.evolve(prog, 1, 6)
+    b.evolve(prog, 6, 16)
+    assert np.array_equal(a.download(), b.download())
+
+
+def test_complex64_error_is_stated(gpu, orc):
+    """complex64 state with FP32 arithmetic (FP64 coefficients rounded once):
+    the amplitudes stay within 2e-5 of the complex128 oracle over 31 powers at
+    n = 12, and the histogram within 1e-5."""
+    q = gpu
+    n, N, P = 12, 6, 5
+    M, e = n // 2, N // 2
+    seg = _seg(q, n, N, 21, 0.05)
+    prog = q.Program(seg, M, e, e)
+    st = q.DeviceState(M, e, e, P, dtype=np.complex64)
+    b0 = q.hf_block0(st.c_alpha, st.c_beta, P)
+    st.upload(b0.astype(np.complex64))
+    st.evolve(prog)
+    got = st.download()
+    ref = np.zeros(st.size, np.complex128)
+    ref[:st.ld] = b0
+    orc.time_evolve(M, e, e, P, seg, ref)
+    err = np.abs(got - ref).max()
+    assert err < 2e-5, err
+    st.qift()
+    orc.qift(P, st.ld, ref)
+    perr = np.abs(st.phase_probs() - orc.identify_phase_amplitudes(P, st.ld, ref)).max()
+    assert perr < 1e-5, perr
+
+
+def test_edge_shapes(gpu, orc):
+    """Full shells (C = 1), a single orbital, no terms at all, and P = 1."""
+    q = gpu
+    from qpesim_gb300 import TERM_DTYPE
+    empty = {k: np.zeros(0, TERM_DTYPE) for k in KINDS}
+    for M, na, nb, P, seg in [(3, 3, 3, 2, _seg(q, 6, 6, 3, 0.1)), (1, 1, 1, 3, _seg(q, 2, 2, 4, 0.3)),
+                              (4, 2, 2, 1, empty), (4, 2, 1, 2, _seg(q, 8, 4, 5, 0.2))]:
+        prog = q.Program(seg, M, na, nb)
+        st = q.DeviceState(M, na, nb, P)
+        b0 = q.hf_block0(st.c_alpha, st.c_beta, P) + 0.1
+        st.upload(b0)
+        st.evolve(prog)
+        ref = np.zeros(st.size, np.complex128)
+        ref[:st.ld] = b0
+        orc.time_evolve(M, na, nb, P, seg, ref)
+        assert np.array_equal(st.download(), ref)
+
+
+def test_invalid_input_is_reported(gpu):
+    q = gpu
+    seg = _seg(q, 8, 4, 1, 0.1)
+    bad = {k: v.copy() for k, v in seg.items()}
+    bad["pq"]["p"][0] = 99
+    with pytest.raises(q.QpeError):
+        q.Program(bad, 4, 2, 2)
+    bad = {k: v.copy() for k, v in seg.items()}
+    bad["pqrs"]["q"][0] = bad["pqrs"]["p"][0]
+    with pytest.raises(q.QpeError):
+        q.Program(bad, 4, 2, 2)
+    with pytest.raises(q.QpeError):
+        q.DeviceState(4, 5, 2, 3)
+    prog = q.Program(seg, 4, 2, 2)
+    st = q.DeviceState(5, 2, 2, 2)
+    with pytest.raises(q.QpeError):
+        st.evolve(prog)  # shapes differ
+    with pytest.raises(q.QpeError):
+        q.OffsetComputer.unrank(8, 4, [70])
+
+
+def test_pp_fixture_phase_on_gpu(gpu):
+    """cpp/time_evolution.hpp:339-367 on the hot path: probs[87] > 0.5."""
+    q = gpu
+    h = q.Hamiltonian()
+    h.SetNumOrbitals(1)
+    h.SetNumOccupied(1)
+    h.AddOneBodyTerm((1, 1), 1.0)
+    h.IndexTerms()
+    h.SetTimestep(1.0)
+    P = 7
+    sv = q.StateVector(P, 1, 1)
+    sv[0] = 2 ** (-P / 2)
+    q.time_evolve_over_terms(sv, h, P)
+    sv.qift()
+    assert sv.IdentifyPhaseAmplitudes()[87] > 0.5
