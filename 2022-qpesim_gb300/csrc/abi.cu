@@ -1,6 +1,7 @@
 // abi.cu - implementation of the C ABI declared in include/qpe_gb300.h.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -72,7 +73,7 @@ struct qpe_program {
   qpe_context* ctx = nullptr;
   uint64_t id = 0;  // unique per process, keys the cached evolution graphs
   HostProgram hp;
-  DevBuf pool, ops, coef, strA, strB, tabs, start;
+  DevBuf pool, ops, coef, strA, strB, tabs, start, passes;
 };
 
 struct qpe_state {
@@ -87,6 +88,10 @@ struct qpe_state {
   // Cached one-power graph for the last program evolved on this state.
   uint64_t graph_prog = 0;
   cudaGraphExec_t graph = nullptr;
+  // Resident-kernel descriptor and the autotuned strategy per program.
+  DevBuf res_inst;
+  uint64_t tuned_prog = 0;
+  uint32_t tuned_strategy = 0, tuned_cluster = 0;
   ~qpe_state() {
     if (graph) cudaGraphExecDestroy(graph);
   }
@@ -153,6 +158,9 @@ static void build_device_program(qpe_program* pr) {
     QPE_CK(cudaMemcpyAsync(pr->ops.p, hp.ops.data(), hp.ops.size() * sizeof(DevOp), cudaMemcpyHostToDevice, s));
   if (!hp.coefs.empty())
     QPE_CK(cudaMemcpyAsync(pr->coef.p, hp.coefs.data(), hp.coefs.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+  pr->passes.alloc(hp.passes.size() * sizeof(Pass));
+  if (!hp.passes.empty())
+    QPE_CK(cudaMemcpyAsync(pr->passes.p, hp.passes.data(), hp.passes.size() * sizeof(Pass), cudaMemcpyHostToDevice, s));
   QPE_CK(launch_line_strings(ctx->binom.as<uint64_t>(), hp.M, hp.na, pr->strA.as<uint32_t>(), (uint32_t)hp.Ca, s));
   QPE_CK(launch_line_strings(ctx->binom.as<uint64_t>(), hp.M, hp.nb, pr->strB.as<uint32_t>(), (uint32_t)hp.Cb, s));
   // Index tables: one thread per entry.
@@ -209,6 +217,147 @@ static PassLaunch plan_pass(const qpe_program* pr, const qpe_state* st, const Pa
   return pl;
 }
 
+static uint32_t pow2_tiles(uint64_t lines, uint64_t want_tiles) {
+  // Largest W in {1, 2, .., 32} with ceil(lines / W) >= want_tiles.
+  uint32_t W = 1;
+  while (W < 32 && (lines + 2 * W - 1) / (2 * W) >= want_tiles) W *= 2;
+  return W;
+}
+
+// Geometry of the resident kernel for cluster size K; false if it does not fit.
+static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K, ResidentLaunch& rl,
+                          ResidentInstance& ri) {
+  const HostProgram& hp = pr->hp;
+  const size_t esz = st->esz;
+  const uint64_t Ca = hp.Ca, Cb = hp.Cb;
+  const uint64_t Rk = (Ca + K - 1) / K;
+  uint32_t mixcount = 0;
+  for (const Pass& p : hp.passes)
+    if (p.type == PASS_MIX) mixcount = std::max(mixcount, p.mixcount);
+  for (uint32_t wpc = 16; wpc >= 4; wpc /= 2) {
+    ri = ResidentInstance{};
+    ri.Ca = (uint32_t)Ca;
+    ri.Cb = (uint32_t)Cb;
+    ri.rows_per_cta = (uint32_t)Rk;
+    ri.Wr = pow2_tiles(Rk, wpc);
+    ri.Wc = pow2_tiles(Cb, (uint64_t)K * wpc);
+    ri.Wm = pow2_tiles(mixcount ? mixcount : 1, (uint64_t)K * wpc);
+    uint64_t stage = 0;
+    if (K > 1) {
+      while (true) {
+        stage = std::max<uint64_t>(Ca * ri.Wc, 2 * Ca * ri.Wm);
+        if (Rk * Cb * esz + wpc * stage * esz <= st->ctx->smem_optin || (ri.Wc == 1 && ri.Wm == 1)) break;
+        if (ri.Wc > 1) ri.Wc /= 2;
+        if (ri.Wm > 1 && 2 * Ca * ri.Wm > Ca * ri.Wc) ri.Wm /= 2;
+      }
+    }
+    const size_t smem = (size_t)(Rk * Cb * esz + wpc * stage * esz);
+    if (smem <= st->ctx->smem_optin) {
+      rl = ResidentLaunch{};
+      rl.ninst = 1;
+      rl.cluster = K;
+      rl.warps_per_cta = wpc;
+      rl.stage_elems = (uint32_t)stage;
+      rl.smem_bytes = smem < 1024 ? 1024 : smem;
+      return true;
+    }
+  }
+  return false;
+}
+
+static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint32_t first, uint32_t last) {
+  ResidentLaunch rl;
+  ResidentInstance ri;
+  if (!plan_resident(pr, st, K, rl, ri)) throw Error(QPE_ERR_UNSUPPORTED, "block does not fit the cluster's shared memory");
+  ri.state = st->data.p;
+  ri.pool = pr->pool.as<uint32_t>();
+  ri.ops = pr->ops.as<DevOp>();
+  ri.coef = pr->coef.as<double>();
+  ri.passes = pr->passes.as<Pass>();
+  ri.strA = pr->strA.as<uint32_t>();
+  ri.strB = pr->strB.as<uint32_t>();
+  ri.npasses = (uint32_t)pr->hp.passes.size();
+  ri.first = first;
+  ri.last = last;
+  if (!st->res_inst.p) st->res_inst.alloc(sizeof(ResidentInstance));
+  QPE_CK(cudaMemcpyAsync(st->res_inst.p, &ri, sizeof(ri), cudaMemcpyHostToDevice, st->ctx->stream));
+  rl.insts = st->res_inst.as<ResidentInstance>();
+  QPE_CK(launch_resident(rl, st->dtype, st->dtype == QPE_C128, st->ctx->stream));
+}
+
+static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last);
+
+// Strategy for (program, state): explicit, or timed on one power per candidate.
+static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts, uint32_t& strategy,
+                            uint32_t& K) {
+  strategy = opts ? opts->strategy : QPE_STRATEGY_AUTO;
+  K = opts ? opts->cluster_size : 0;
+  ResidentLaunch rl;
+  ResidentInstance ri;
+  if (strategy == QPE_STRATEGY_RESIDENT) {
+    K = 1;
+    return;
+  }
+  if (strategy == QPE_STRATEGY_CLUSTER) {
+    if (K == 0) {
+      for (uint32_t c = 2; c <= 16 && !K; c *= 2)
+        if (plan_resident(pr, st, c, rl, ri)) K = c;
+      if (!K) throw Error(QPE_ERR_UNSUPPORTED, "block does not fit a cluster of 16");
+    }
+    return;
+  }
+  if (strategy == QPE_STRATEGY_TILED) return;
+  if (st->tuned_prog == pr->id) {
+    strategy = st->tuned_strategy;
+    K = st->tuned_cluster;
+    return;
+  }
+  // Autotune: time one power of every feasible candidate (block 1 is rewritten
+  // by the real run afterwards).
+  std::vector<std::pair<uint32_t, uint32_t>> cands;
+  for (uint32_t c = 1; c <= 16; c *= 2)
+    if (plan_resident(pr, st, c, rl, ri)) cands.push_back({c == 1 ? QPE_STRATEGY_RESIDENT : QPE_STRATEGY_CLUSTER, c});
+  if (cands.empty()) {
+    strategy = QPE_STRATEGY_TILED;
+  } else if (cands.size() == 1) {
+    strategy = cands[0].first;
+    K = cands[0].second;
+  } else {
+    cudaEvent_t e0, e1;
+    QPE_CK(cudaEventCreate(&e0));
+    QPE_CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (auto& c : cands) {
+      float ms = 0;
+      try {
+        run_resident(st, pr, c.second, 1, 2);  // warm-up of this configuration
+        QPE_CK(cudaEventRecord(e0, st->ctx->stream));
+        run_resident(st, pr, c.second, 1, 2);
+        QPE_CK(cudaEventRecord(e1, st->ctx->stream));
+        QPE_CK(cudaEventSynchronize(e1));
+        QPE_CK(cudaEventElapsedTime(&ms, e0, e1));
+      } catch (const Error&) {
+        // A configuration the device cannot launch (e.g. too many CTAs per
+        // cluster for the resources) is skipped; a sticky fault is not.
+        if (cudaPeekAtLastError() != cudaSuccess) cudaGetLastError();
+        if (cudaStreamQuery(st->ctx->stream) != cudaSuccess && cudaStreamQuery(st->ctx->stream) != cudaErrorNotReady) throw;
+        continue;
+      }
+      if (ms < best) {
+        best = ms;
+        strategy = c.first;
+        K = c.second;
+      }
+    }
+    if (best == 1e30f) strategy = QPE_STRATEGY_TILED;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  st->tuned_prog = pr->id;
+  st->tuned_strategy = strategy;
+  st->tuned_cluster = K;
+}
+
 static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts) {
   const HostProgram& hp = pr->hp;
   if (hp.M != st->M || hp.na != st->na || hp.nb != st->nb)
@@ -219,6 +368,22 @@ static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* 
     last = opts->last_power;
   }
   if (first < 1 || last > st->N || first > last) throw Error(QPE_ERR_INVALID, "power range outside 1 .. 2^P");
+  st->probs_valid = false;
+  if (first == last) return;
+  uint32_t strategy = 0, K = 0;
+  choose_strategy(st, pr, opts, strategy, K);
+  if (strategy == QPE_STRATEGY_TILED) {
+    evolve_tiled(st, pr, first, last);
+  } else {
+    run_resident(st, pr, K, first, last);
+    QPE_CK(cudaStreamSynchronize(st->ctx->stream));
+  }
+}
+
+// Global-memory working block, one kernel launch per pass, one captured graph
+// per controlled power replayed for every power.
+static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last) {
+  const HostProgram& hp = pr->hp;
   cudaStream_t s = st->ctx->stream;
   if (!st->work.p) st->work.alloc(st->ld * st->esz);
   // Working block <- block first - 1.
@@ -226,11 +391,6 @@ static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* 
                          st->ld * st->esz, cudaMemcpyDeviceToDevice, s));
   k_set_int<<<1, 1, 0, s>>>(st->dk.as<int>(), (int)first);
   QPE_CK(cudaGetLastError());
-  st->probs_valid = false;
-  if (first == last) {
-    QPE_CK(cudaStreamSynchronize(s));
-    return;
-  }
   if (st->graph_prog != pr->id || !st->graph) {
     if (st->graph) cudaGraphExecDestroy(st->graph);
     st->graph = nullptr;
@@ -661,8 +821,9 @@ int qpe_evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts
   return guard([&] {
     check_state(st);
     if (!pr) throw Error(QPE_ERR_INVALID, "null program");
-    if (opts && opts->strategy != QPE_STRATEGY_AUTO && opts->strategy != QPE_STRATEGY_TILED)
-      throw Error(QPE_ERR_UNSUPPORTED, "strategy not available");
+    if (opts && opts->strategy > QPE_STRATEGY_TILED) throw Error(QPE_ERR_INVALID, "unknown strategy");
+    if (opts && opts->cluster_size && (opts->cluster_size > 16 || (opts->cluster_size & (opts->cluster_size - 1))))
+      throw Error(QPE_ERR_INVALID, "cluster_size must be a power of two <= 16");
     evolve(st, pr, opts);
   });
 }

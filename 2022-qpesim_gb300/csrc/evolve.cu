@@ -17,102 +17,11 @@
 #include <stdint.h>
 
 #include "kernels.h"
+#include "tile_ops.cuh"
 
 namespace qpe {
 
-template <typename R>
-struct Cx;
-template <>
-struct Cx<double> {
-  using T = double2;
-};
-template <>
-struct Cx<float> {
-  using T = float2;
-};
-
-// Arithmetic policies. Exact: separate IEEE roundings (no FMA), the order of
-// std::complex<double>'s (ac - bd, ad + bc). Fast: contraction allowed.
-struct ExactD {
-  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-};
-template <typename R>
-struct Fast {
-  static __device__ __forceinline__ R mul(R a, R b) { return a * b; }
-  static __device__ __forceinline__ R add(R a, R b) { return a + b; }
-  static __device__ __forceinline__ R sub(R a, R b) { return a - b; }
-};
-
-template <typename R>
-struct Coef4 {
-  R e0r, e0i, e1r, e1i, o0r, o0i, o1r, o1i;
-  bool reduced;  // m00 real and m01 imaginary for both parities
-};
-
-template <typename R>
-__device__ __forceinline__ Coef4<R> load_coef(const double* __restrict__ c) {
-  Coef4<R> k;
-  k.e0r = (R)__ldg(c + 0);
-  k.e0i = (R)__ldg(c + 1);
-  k.e1r = (R)__ldg(c + 2);
-  k.e1i = (R)__ldg(c + 3);
-  k.o0r = (R)__ldg(c + 4);
-  k.o0i = (R)__ldg(c + 5);
-  k.o1r = (R)__ldg(c + 6);
-  k.o1i = (R)__ldg(c + 7);
-  k.reduced = __ldg(c + 1) == 0.0 && __ldg(c + 2) == 0.0 && __ldg(c + 5) == 0.0 && __ldg(c + 6) == 0.0;
-  return k;
-}
-
-// Full complex product a * b in the reference's operation order.
-template <class A, typename R>
-__device__ __forceinline__ void cmul(R ar, R ai, R br, R bi, R& outr, R& outi) {
-  outr = A::sub(A::mul(ar, br), A::mul(ai, bi));
-  outi = A::add(A::mul(ar, bi), A::mul(ai, br));
-}
-
-template <class A, typename C2, typename R>
-__device__ __forceinline__ void pair_update(C2& l, C2& r, const Coef4<R>& k, uint32_t par) {
-  const R m0r = par ? k.o0r : k.e0r, m0i = par ? k.o0i : k.e0i;
-  const R m1r = par ? k.o1r : k.e1r, m1i = par ? k.o1i : k.e1i;
-  const C2 vl = l, vr = r;
-  if (k.reduced) {
-    // m00 = (c, 0), m01 = (0, t): l' = (lx c - ry t, ly c + rx t), r' = (rx c - ly t, lx t + ry c).
-    l.x = A::sub(A::mul(vl.x, m0r), A::mul(vr.y, m1i));
-    l.y = A::add(A::mul(vl.y, m0r), A::mul(vr.x, m1i));
-    r.x = A::sub(A::mul(vr.x, m0r), A::mul(vl.y, m1i));
-    r.y = A::add(A::mul(vl.x, m1i), A::mul(vr.y, m0r));
-  } else {
-    R ar, ai, br, bi;
-    cmul<A>(vl.x, vl.y, m0r, m0i, ar, ai);
-    cmul<A>(vr.x, vr.y, m1r, m1i, br, bi);
-    l.x = A::add(ar, br);
-    l.y = A::add(ai, bi);
-    cmul<A>(vl.x, vl.y, m1r, m1i, ar, ai);
-    cmul<A>(vr.x, vr.y, m0r, m0i, br, bi);
-    r.x = A::add(ar, br);
-    r.y = A::add(ai, bi);
-  }
-}
-
-template <class A, typename C2, typename R>
-__device__ __forceinline__ void diag_update(C2& v, const Coef4<R>& k) {
-  R xr, xi;
-  cmul<A>(v.x, v.y, k.e0r, k.e0i, xr, xi);
-  v.x = xr;
-  v.y = xi;
-}
-
-__device__ __forceinline__ bool cond_ok(uint32_t line_str, const DevOp& op) {
-  uint32_t m = 0;
-  if (op.ncond > 0) m |= 1u << op.cb0;
-  if (op.ncond > 1) m |= 1u << op.cb1;
-  return (line_str & m) == m;
-}
-
-// One pass. PT selects the tile geometry:
+// One pass. PT selects the tile geometry (stage layout [entry][line]):
 //   PASS_COL: tile = W consecutive columns, stage[e * W + w] = block[e][b0 + w]
 //   PASS_ROW: tile = one row,               stage[e]         = block[a][e]
 //   PASS_MIX: tile = columns (b01, b10),    stage[e * 2 + w] = block[e][w ? b10 : b01]
@@ -140,14 +49,12 @@ __global__ void k_pass(PassLaunch pl) {
     if (PT == PASS_COL) b0 = tile << logW;
     if (PT == PASS_ROW) row = tile;
     if (PT == PASS_MIX) {
-      const uint32_t x = __ldg(pool + pl.pass.mixtab + 2 * tile);
-      b10 = __ldg(pool + pl.pass.mixtab + 2 * tile + 1);
-      b01 = x & 0x7fffffffu;
-      parb = x >> 31;
+      const uint2 x = __ldg(reinterpret_cast<const uint2*>(pool + pl.pass.mixtab) + tile);
+      b01 = x.x & 0x7fffffffu;
+      b10 = x.y;
+      parb = x.x >> 31;
     }
     const uint32_t nl = (PT == PASS_COL) ? min(W, Cb - b0) : W;  // valid lines
-    // Line strings for the terms' occupation conditions (at most 32 lines / lane).
-    // gather
     for (uint32_t i = lane; i < L * W; i += 32) {
       const uint32_t e = i >> logW, w = i & (W - 1);
       if (w >= nl) continue;
@@ -158,53 +65,19 @@ __global__ void k_pass(PassLaunch pl) {
       st[i] = blk[g];
     }
     __syncwarp();
-    for (uint32_t o = pl.pass.op0; o < pl.pass.op1; ++o) {
-      const DevOp op = pl.ops[o];
-      const Coef4<R> k = load_coef<R>(pl.coef + 8 * (size_t)op.coef);
-      if (PT == PASS_MIX) {
-        // ABBA: pair (a01 on column b01) <-> (a10 on column b10); parity adds the
-        // beta pair's parity (:774).
-        for (uint32_t j = lane; j < op.count; j += 32) {
-          const uint32_t x = __ldg(pool + op.tab + 2 * j);
-          const uint32_t a10 = __ldg(pool + op.tab + 2 * j + 1);
-          const uint32_t a01 = x & 0x7fffffffu;
-          pair_update<A>(st[a01 * 2 + 0], st[a10 * 2 + 1], k, (x >> 31) ^ parb);
-        }
-      } else {
-        const uint32_t* __restrict__ lstr = (PT == PASS_COL) ? pl.strB : pl.strA;
-        const uint32_t line0 = (PT == PASS_COL) ? b0 : row;
-        if (op.kind == OPK_PAIR) {
-          const uint32_t n = op.count << logW;
-          for (uint32_t i = lane; i < n; i += 32) {
-            const uint32_t j = i >> logW, w = i & (W - 1);
-            if (w >= nl) continue;
-            if (op.ncond && !cond_ok(__ldg(lstr + line0 + w), op)) continue;
-            const uint32_t x = __ldg(pool + op.tab + 2 * j);
-            const uint32_t y = __ldg(pool + op.tab + 2 * j + 1);
-            pair_update<A>(st[((x & 0x7fffffffu) << logW) + w], st[(y << logW) + w], k, x >> 31);
-          }
-        } else if (op.kind == OPK_DIAG_LIST) {
-          const uint32_t n = op.count << logW;
-          for (uint32_t i = lane; i < n; i += 32) {
-            const uint32_t j = i >> logW, w = i & (W - 1);
-            if (w >= nl) continue;
-            if (op.ncond && !cond_ok(__ldg(lstr + line0 + w), op)) continue;
-            const uint32_t e = __ldg(pool + op.tab + j);
-            diag_update<A>(st[(e << logW) + w], k);
-          }
-        } else {  // OPK_DIAG_ALL
-          const uint32_t n = L << logW;
-          for (uint32_t i = lane; i < n; i += 32) {
-            const uint32_t w = i & (W - 1);
-            if (w >= nl) continue;
-            if (op.ncond && !cond_ok(__ldg(lstr + line0 + w), op)) continue;
-            diag_update<A>(st[i], k);
-          }
-        }
-      }
-      __syncwarp();
+    if (PT == PASS_MIX) {
+      run_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, lane, 32, true, parb,
+                        [&](uint32_t a) -> C2& { return st[2 * a]; },
+                        [&](uint32_t a) -> C2& { return st[2 * a + 1]; });
+    } else {
+      // Lane l owns line l % W and walks entries l / W, l / W + 32 / W, ...
+      const uint32_t w = lane & (W - 1);
+      const bool active = w < nl;
+      const uint32_t line = (PT == PASS_COL) ? b0 + w : row;
+      const uint32_t lstr = active ? __ldg(((PT == PASS_COL) ? pl.strB : pl.strA) + line) : 0u;
+      run_line_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, L, lane >> logW, 32 >> logW, active, lstr,
+                         [&](uint32_t e) -> C2& { return st[(e << logW) + w]; });
     }
-    // scatter
     for (uint32_t i = lane; i < L * W; i += 32) {
       const uint32_t e = i >> logW, w = i & (W - 1);
       if (w >= nl) continue;

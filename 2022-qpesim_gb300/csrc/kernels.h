@@ -48,6 +48,33 @@ cudaError_t launch_snapshot(const void* work, void* state, uint64_t block_elems,
 cudaError_t launch_advance(int* d_k, cudaStream_t s);
 cudaError_t configure_pass_kernels(int dtype, size_t smem_bytes);
 
+// ---- resident evolution (resident.cu) ----
+// One instance of the resident kernel: its register in global memory and its
+// compiled program. Lines per tile Wc / Wr / Wm are powers of two dividing 32.
+struct ResidentInstance {
+  void* state;
+  const uint32_t* pool;
+  const DevOp* ops;
+  const double* coef;
+  const Pass* passes;
+  const uint32_t* strA;
+  const uint32_t* strB;
+  uint32_t Ca, Cb, npasses;
+  uint32_t first, last;     // powers evolved: blocks first .. last - 1
+  uint32_t rows_per_cta;    // rows owned by each CTA of the cluster
+  uint32_t Wc, Wr, Wm;
+};
+struct ResidentLaunch {
+  const ResidentInstance* insts;  // device array, ninst entries
+  uint32_t ninst;
+  uint32_t cluster;               // CTAs per instance (1 = one CTA)
+  uint32_t warps_per_cta;
+  uint32_t stage_elems;           // per-warp stage (cluster > 1)
+  size_t smem_bytes;
+};
+cudaError_t launch_resident(const ResidentLaunch& rl, int dtype, int exact, cudaStream_t s);
+cudaError_t resident_max_cluster(int dtype, uint32_t cluster, uint32_t warps, size_t smem, int* max_clusters);
+
 // ---- QIFT and reductions (qift.cu) ----
 cudaError_t launch_qift(void* state, uint64_t ld, uint32_t P, const void* twiddles, double norm, double* partial,
                         uint32_t grid, uint32_t cols_per_cta, int dtype, cudaStream_t s);

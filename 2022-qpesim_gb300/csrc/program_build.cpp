@@ -63,6 +63,7 @@ struct Builder {
     t.count = (uint32_t)cnt;
     const bool pairs = kind == AX_CA || kind == AX_CNA || kind == AX_CCAA;
     uint64_t words = cnt * (pairs ? 2 : 1);
+    if (pairs && (P.pool_words & 1)) ++P.pool_words;  // pair entries are read as 8-byte words
     if (P.pool_words + words > 0xffffffffull) throw Error(QPE_ERR_UNSUPPORTED, "index pool too large");
     t.offset = (uint32_t)P.pool_words;
     P.pool_words += words;

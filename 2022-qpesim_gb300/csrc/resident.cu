@@ -1,0 +1,219 @@
+// resident.cu - the evolution with the working block resident in shared memory.
+//
+// One launch runs every controlled power of one or more instances. An instance
+// is owned by one CTA (K = 1) or by a thread-block cluster of K CTAs whose
+// shared memories together hold the Ca x Cb block, split by rows: CTA r of the
+// cluster owns rows [r * Rk, (r + 1) * Rk). For every pass of a power the
+// cluster's warps take the pass's tiles (program.h):
+//   K = 1: tiles are processed in place in shared memory;
+//   K > 1: row tiles are local to the CTA that owns the rows; column and
+//          column-pair tiles are gathered from the cluster's shared memories
+//          (distributed shared memory) into a warp-private stage, processed,
+//          and scattered back.
+// A barrier (__syncthreads for K = 1, the cluster barrier otherwise) closes
+// every pass. After a power each CTA copies its rows to block k of the register
+// in global memory (the copy of cpp/time_evolution_over_terms.hpp:130-132, taken
+// after the power), so block k = U^k block 0. No thread waits on a flag: the
+// only synchronisation is the hardware barrier, reached the same number of
+// times by every CTA of the cluster.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.h"
+#include "tile_ops.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace qpe {
+
+template <typename C2>
+__device__ __forceinline__ C2* cta_ptr(C2* local, uint32_t rank, uint32_t K) {
+  if (K == 1) return local;
+  return cg::this_cluster().map_shared_rank(local, rank);
+}
+
+template <typename R, class A>
+__global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __restrict__ insts, uint32_t stage_elems) {
+  using C2 = typename Cx<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t K = cl.num_blocks();
+  const uint32_t rank = cl.block_rank();
+  const ResidentInstance I = insts[blockIdx.x / K];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpc = blockDim.x >> 5;
+  const uint32_t Ca = I.Ca, Cb = I.Cb, Rk = I.rows_per_cta;
+  const uint32_t row0 = min(rank * Rk, Ca), row1 = min(row0 + Rk, Ca);
+  C2* blk = reinterpret_cast<C2*>(smem_raw);
+  C2* stage = blk + (size_t)Rk * Cb + (size_t)warp * stage_elems;
+  C2* __restrict__ gstate = reinterpret_cast<C2*>(I.state);
+  const uint64_t ld = (uint64_t)Ca * Cb;
+  const uint32_t nown = (row1 - row0) * Cb;
+
+  auto barrier = [&]() {
+    if (K == 1) __syncthreads();
+    else cl.sync();
+  };
+  // Generic pointer to element (a, b) of the cluster-distributed block.
+  auto at = [&](uint32_t a, uint32_t b) -> C2* {
+    const uint32_t r = a / Rk;
+    return cta_ptr(blk, r, K) + (size_t)(a - r * Rk) * Cb + b;
+  };
+
+  // Block first - 1 into shared memory.
+  {
+    const C2* src = gstate + (uint64_t)(I.first - 1) * ld + (uint64_t)row0 * Cb;
+    for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) blk[i] = src[i];
+  }
+  barrier();
+
+  for (uint32_t k = I.first; k < I.last; ++k) {
+    for (uint32_t pi = 0; pi < I.npasses; ++pi) {
+      const Pass P = I.passes[pi];
+      if (P.type == PASS_ROW) {
+        // Rows owned by this CTA, Wr rows per warp tile, in place.
+        const uint32_t W = I.Wr, logW = __ffs(W) - 1, w = lane & (W - 1);
+        const uint32_t jl = lane >> logW, jstep = 32 >> logW;
+        const uint32_t ntiles = (row1 - row0 + W - 1) >> logW;
+        for (uint32_t tile = warp; tile < ntiles; tile += wpc) {
+          const uint32_t r = row0 + (tile << logW) + w;
+          const bool active = r < row1;
+          const uint32_t lstr = active ? __ldg(I.strA + r) : 0u;
+          C2* line = blk + (size_t)(active ? r - row0 : 0) * Cb;
+          run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, Cb, jl, jstep, active, lstr,
+                             [&](uint32_t e) -> C2& { return line[e]; });
+        }
+      } else if (P.type == PASS_COL) {
+        const uint32_t W = I.Wc, logW = __ffs(W) - 1, w = lane & (W - 1);
+        const uint32_t jl = lane >> logW, jstep = 32 >> logW;
+        const uint32_t ntiles = (Cb + W - 1) >> logW;
+        const uint32_t gw = rank * wpc + warp, nw = K * wpc;
+        for (uint32_t tile = gw; tile < ntiles; tile += nw) {
+          const uint32_t b0 = tile << logW, c = b0 + w;
+          const bool active = c < Cb;
+          const uint32_t lstr = active ? __ldg(I.strB + c) : 0u;
+          if (K == 1) {
+            C2* col = blk + (active ? c : 0);
+            run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, Ca, jl, jstep, active, lstr,
+                               [&](uint32_t e) -> C2& { return col[(size_t)e * Cb]; });
+          } else {
+            const uint32_t nl = min(W, Cb - b0);
+            for (uint32_t i = lane; i < (Ca << logW); i += 32) {
+              const uint32_t e = i >> logW, ww = i & (W - 1);
+              if (ww < nl) stage[i] = *at(e, b0 + ww);
+            }
+            __syncwarp();
+            run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, Ca, jl, jstep, active, lstr,
+                               [&](uint32_t e) -> C2& { return stage[(e << logW) + w]; });
+            for (uint32_t i = lane; i < (Ca << logW); i += 32) {
+              const uint32_t e = i >> logW, ww = i & (W - 1);
+              if (ww < nl) *at(e, b0 + ww) = stage[i];
+            }
+            __syncwarp();
+          }
+        }
+      } else {  // PASS_MIX: Wm column pairs per tile
+        const uint32_t W = I.Wm, logW = __ffs(W) - 1, w = lane & (W - 1);
+        const uint32_t jl = lane >> logW, jstep = 32 >> logW;
+        const uint32_t ntiles = (P.mixcount + W - 1) >> logW;
+        const uint32_t gw = rank * wpc + warp, nw = K * wpc;
+        const uint2* __restrict__ mt = reinterpret_cast<const uint2*>(I.pool + P.mixtab);
+        for (uint32_t tile = gw; tile < ntiles; tile += nw) {
+          const uint32_t t0 = tile << logW, t = t0 + w;
+          const bool active = t < P.mixcount;
+          const uint2 bp = active ? __ldg(mt + t) : make_uint2(0u, 0u);
+          const uint32_t b01 = bp.x & 0x7fffffffu, b10 = bp.y, parb = bp.x >> 31;
+          if (K == 1) {
+            run_mix_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, jl, jstep, active, parb,
+                              [&](uint32_t a) -> C2& { return blk[(size_t)a * Cb + b01]; },
+                              [&](uint32_t a) -> C2& { return blk[(size_t)a * Cb + b10]; });
+          } else {
+            const uint32_t nl = min(W, P.mixcount - t0);
+            const uint32_t n2 = Ca << (logW + 1);
+            for (uint32_t i = lane; i < n2; i += 32) {
+              const uint32_t a = i >> (logW + 1), ww = (i >> 1) & (W - 1), side = i & 1;
+              if (ww < nl) {
+                const uint2 q = __ldg(mt + t0 + ww);
+                stage[i] = *at(a, side ? q.y : (q.x & 0x7fffffffu));
+              }
+            }
+            __syncwarp();
+            run_mix_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, jl, jstep, active, parb,
+                              [&](uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w]; },
+                              [&](uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w + 1]; });
+            for (uint32_t i = lane; i < n2; i += 32) {
+              const uint32_t a = i >> (logW + 1), ww = (i >> 1) & (W - 1), side = i & 1;
+              if (ww < nl) {
+                const uint2 q = __ldg(mt + t0 + ww);
+                *at(a, side ? q.y : (q.x & 0x7fffffffu)) = stage[i];
+              }
+            }
+            __syncwarp();
+          }
+        }
+      }
+      barrier();
+    }
+    // Snapshot of this CTA's rows into block k.
+    C2* dst = gstate + (uint64_t)k * ld + (uint64_t)row0 * Cb;
+    for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) dst[i] = blk[i];
+    barrier();
+  }
+}
+
+template <typename R, class A>
+static cudaError_t launch_res(const ResidentLaunch& rl, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(rl.ninst * rl.cluster);
+  cfg.blockDim = dim3(32 * rl.warps_per_cta);
+  cfg.dynamicSmemBytes = rl.smem_bytes;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = rl.cluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaFuncSetAttribute(k_resident<R, A>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)rl.smem_bytes);
+  if (e) return e;
+  if (rl.cluster > 8) {
+    e = cudaFuncSetAttribute(k_resident<R, A>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e) return e;
+  }
+  e = cudaLaunchKernelEx(&cfg, k_resident<R, A>, rl.insts, rl.stage_elems);
+  return e;
+}
+
+cudaError_t launch_resident(const ResidentLaunch& rl, int dtype, int exact, cudaStream_t s) {
+  if (dtype == QPE_C128) {
+    if (exact) return launch_res<double, ExactD>(rl, s);
+    return launch_res<double, Fast<double>>(rl, s);
+  }
+  return launch_res<float, Fast<float>>(rl, s);
+}
+
+cudaError_t resident_max_cluster(int dtype, uint32_t cluster, uint32_t warps, size_t smem, int* max_clusters) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cluster);
+  cfg.blockDim = dim3(32 * warps);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (dtype == QPE_C128) {
+    cudaFuncSetAttribute(k_resident<double, ExactD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cluster > 8) cudaFuncSetAttribute(k_resident<double, ExactD>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return cudaOccupancyMaxActiveClusters(max_clusters, k_resident<double, ExactD>, &cfg);
+  }
+  cudaFuncSetAttribute(k_resident<float, Fast<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cluster > 8) cudaFuncSetAttribute(k_resident<float, Fast<float>>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return cudaOccupancyMaxActiveClusters(max_clusters, k_resident<float, Fast<float>>, &cfg);
+}
+
+}  // namespace qpe

@@ -119,8 +119,12 @@ class DeviceState:
     def zero(self) -> None:
         N.check(self._lib.qpe_state_zero(self._h))
 
-    def evolve(self, program: Program, first_power: int = 0, last_power: int = 0, strategy: int = 0) -> None:
-        opts = N.EvolveOpts(strategy, first_power, last_power, 0)
+    def evolve(self, program: Program, first_power: int = 0, last_power: int = 0, strategy: int = 0,
+               cluster_size: int = 0) -> None:
+        """strategy: 0 auto (autotuned per program), 1 one CTA resident in shared
+        memory, 2 a cluster of cluster_size CTAs (0: smallest that fits), 3
+        global-memory tile passes."""
+        opts = N.EvolveOpts(strategy, first_power, last_power, cluster_size)
         N.check(self._lib.qpe_evolve(self._h, program._h, C.byref(opts)))
 
     def qift(self) -> None:

@@ -188,8 +188,11 @@ def run_ours(args, w, rank, ws, local):
     timer = N.Timer(local)
     lib = N.lib()
 
+    def evolve():
+        st.evolve(prog, strategy=args.strategy, cluster_size=args.cluster)
+
     def step():
-        st.evolve(prog)
+        evolve()
         st.qift()
         return st.phase_probs()
 
@@ -205,7 +208,7 @@ def run_ours(args, w, rank, ws, local):
         st.upload(block0)
         N.check(lib.qpe_flush_l2(ctx))
         timer.record(0)
-        st.evolve(prog)
+        evolve()
         timer.record(1)
         st.qift()
         probs = st.phase_probs()
@@ -227,7 +230,7 @@ def run_ours(args, w, rank, ws, local):
         N.check(lib.qpe_flush_l2(ctx))
         timer.record(3)
         st.upload(pin_in.array)
-        st.evolve(prog)
+        evolve()
         st.qift()
         probs_host[:] = st.phase_probs()
         st.download(out=pin_out.array)
@@ -322,6 +325,8 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--strategy", type=int, default=0, help="0 auto, 1 one-CTA resident, 2 cluster, 3 tiled")
+    ap.add_argument("--cluster", type=int, default=0, help="CTAs per cluster for --strategy 2 (0: smallest)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

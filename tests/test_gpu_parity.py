@@ -218,3 +218,42 @@ def test_pp_fixture_phase_on_gpu(gpu):
     q.time_evolve_over_terms(sv, h, P)
     sv.qift()
     assert sv.IdentifyPhaseAmplitudes()[87] > 0.5
+
+
+@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 2), (2, 4), (2, 8), (2, 16), (3, 0), (0, 0)])
+@pytest.mark.parametrize("n,na,nb,P", [(12, 3, 3, 3), (14, 4, 3, 2), (8, 2, 2, 4)])
+def test_strategies_bit_identical(gpu, orc, strategy, cluster, n, na, nb, P):
+    """Every evolution strategy (one CTA resident in shared memory, clusters of 2
+    to 16 CTAs over distributed shared memory, global-memory tile passes, and the
+    autotuned choice) gives the oracle's complex128 register bit for bit."""
+    q = gpu
+    M = n // 2
+    seg = _seg(q, n, 2 * max(na, nb), 300 + n, 0.09)
+    prog = q.Program(seg, M, na, nb)
+    st = q.DeviceState(M, na, nb, P)
+    rng = np.random.default_rng(7)
+    b0 = (rng.standard_normal(st.ld) + 1j * rng.standard_normal(st.ld)) / np.sqrt(2 * st.ld)
+    st.upload(b0)
+    opts = dict(strategy=strategy)
+    st.evolve(prog, **opts) if cluster == 0 else st.evolve(prog, strategy=strategy, cluster_size=cluster)
+    ref = np.zeros(st.size, np.complex128)
+    ref[:st.ld] = b0
+    orc.time_evolve(M, na, nb, P, seg, ref)
+    assert np.array_equal(st.download(), ref)
+
+
+@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0)])
+def test_strategies_complex64(gpu, orc, strategy, cluster):
+    q = gpu
+    n, N, P = 12, 6, 4
+    M, e = n // 2, N // 2
+    seg = _seg(q, n, N, 31, 0.05)
+    prog = q.Program(seg, M, e, e)
+    st = q.DeviceState(M, e, e, P, dtype=np.complex64)
+    b0 = q.hf_block0(st.c_alpha, st.c_beta, P)
+    st.upload(b0.astype(np.complex64))
+    st.evolve(prog, strategy=strategy, cluster_size=cluster)
+    ref = np.zeros(st.size, np.complex128)
+    ref[:st.ld] = b0
+    orc.time_evolve(M, e, e, P, seg, ref)
+    assert np.abs(st.download() - ref).max() < 2e-5
