@@ -43,7 +43,7 @@ class ProgramInfo(C.Structure):
 
 class EvolveOpts(C.Structure):
     _fields_ = [("strategy", C.c_uint32), ("first_power", C.c_uint32), ("last_power", C.c_uint32),
-                ("cluster_size", C.c_uint32)]
+                ("cluster_size", C.c_uint32), ("flags", C.c_uint32)]
 
 
 TERM_DTYPE = np.dtype([("p", "<u4"), ("q", "<u4"), ("r", "<u4"), ("s", "<u4"),

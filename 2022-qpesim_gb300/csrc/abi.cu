@@ -87,10 +87,12 @@ struct qpe_state {
   bool probs_valid = false;
   // Cached one-power graph for the last program evolved on this state.
   uint64_t graph_prog = 0;
+  uint32_t graph_exact = 1;
   cudaGraphExec_t graph = nullptr;
   // Resident-kernel descriptor and the autotuned strategy per program.
   DevBuf res_inst;
   uint64_t tuned_prog = 0;
+  uint32_t tuned_exact = 1;
   uint32_t tuned_strategy = 0, tuned_cluster = 0;
   ~qpe_state() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -217,11 +219,24 @@ static PassLaunch plan_pass(const qpe_program* pr, const qpe_state* st, const Pa
   return pl;
 }
 
-static uint32_t pow2_tiles(uint64_t lines, uint64_t want_tiles) {
-  // Largest W in {1, 2, .., 32} with ceil(lines / W) >= want_tiles.
-  uint32_t W = 1;
-  while (W < 32 && (lines + 2 * W - 1) / (2 * W) >= want_tiles) W *= 2;
-  return W;
+// Lines per warp tile W in {1, 2, .., 32}: lane l owns line l % W and walks table
+// entries l / W, l / W + 32 / W, ... Minimises (rounds of tiles over the warps) x
+// (entries per lane of a typical table); ties go to the smaller stage.
+static uint32_t choose_lines(uint64_t lines, uint64_t nwarps, uint64_t entries) {
+  uint32_t best = 1;
+  uint64_t best_cost = ~0ull;
+  for (uint32_t W = 1; W <= 32; W *= 2) {
+    const uint64_t tiles = (lines + W - 1) / W;
+    const uint64_t rounds = (tiles + nwarps - 1) / nwarps;
+    const uint64_t iters = (entries * W + 31) / 32;
+    const uint64_t cost = rounds * (iters ? iters : 1);
+    if (cost < best_cost) {
+      best_cost = cost;
+      best = W;
+    }
+    if (tiles <= 1) break;
+  }
+  return best;
 }
 
 // Geometry of the resident kernel for cluster size K; false if it does not fit.
@@ -239,9 +254,11 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
     ri.Ca = (uint32_t)Ca;
     ri.Cb = (uint32_t)Cb;
     ri.rows_per_cta = (uint32_t)Rk;
-    ri.Wr = pow2_tiles(Rk, wpc);
-    ri.Wc = pow2_tiles(Cb, (uint64_t)K * wpc);
-    ri.Wm = pow2_tiles(mixcount ? mixcount : 1, (uint64_t)K * wpc);
+    // typical table lengths: CA over alpha (COL / MIX), CA over beta (ROW)
+    const uint64_t ea = binom((int)hp.M - 2, (int)hp.na - 1), eb = binom((int)hp.M - 2, (int)hp.nb - 1);
+    ri.Wr = choose_lines(Rk, wpc, eb ? eb : 1);
+    ri.Wc = choose_lines(Cb, (uint64_t)K * wpc, ea ? ea : 1);
+    ri.Wm = choose_lines(mixcount ? mixcount : 1, (uint64_t)K * wpc, ea ? ea : 1);
     uint64_t stage = 0;
     if (K > 1) {
       while (true) {
@@ -265,7 +282,8 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
   return false;
 }
 
-static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint32_t first, uint32_t last) {
+static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint32_t first, uint32_t last,
+                         bool exact) {
   ResidentLaunch rl;
   ResidentInstance ri;
   if (!plan_resident(pr, st, K, rl, ri)) throw Error(QPE_ERR_UNSUPPORTED, "block does not fit the cluster's shared memory");
@@ -279,17 +297,23 @@ static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint3
   ri.npasses = (uint32_t)pr->hp.passes.size();
   ri.first = first;
   ri.last = last;
+  ri.steps = pr->hp.steps;
+  ri.order = pr->hp.order;
   if (!st->res_inst.p) st->res_inst.alloc(sizeof(ResidentInstance));
   QPE_CK(cudaMemcpyAsync(st->res_inst.p, &ri, sizeof(ri), cudaMemcpyHostToDevice, st->ctx->stream));
   rl.insts = st->res_inst.as<ResidentInstance>();
-  QPE_CK(launch_resident(rl, st->dtype, st->dtype == QPE_C128, st->ctx->stream));
+  // Leave the rest of the unified L1 / shared memory to L1, which then holds the
+  // program's terms and index tables across passes.
+  const int pct = (int)std::min<size_t>(100, (rl.smem_bytes * 100 + st->ctx->smem_optin - 1) / st->ctx->smem_optin + 1);
+  QPE_CK(set_resident_carveout(st->dtype, exact, pct));
+  QPE_CK(launch_resident(rl, st->dtype, exact, st->ctx->stream));
 }
 
-static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last);
+static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last, bool exact);
 
 // Strategy for (program, state): explicit, or timed on one power per candidate.
-static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts, uint32_t& strategy,
-                            uint32_t& K) {
+static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts, bool exact,
+                            uint32_t& strategy, uint32_t& K) {
   strategy = opts ? opts->strategy : QPE_STRATEGY_AUTO;
   K = opts ? opts->cluster_size : 0;
   ResidentLaunch rl;
@@ -307,21 +331,19 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     return;
   }
   if (strategy == QPE_STRATEGY_TILED) return;
-  if (st->tuned_prog == pr->id) {
+  if (st->tuned_prog == pr->id && st->tuned_exact == (uint32_t)exact) {
     strategy = st->tuned_strategy;
     K = st->tuned_cluster;
     return;
   }
   // Autotune: time one power of every feasible candidate (block 1 is rewritten
-  // by the real run afterwards).
+  // by the real run afterwards), the tiled strategy included.
   std::vector<std::pair<uint32_t, uint32_t>> cands;
   for (uint32_t c = 1; c <= 16; c *= 2)
     if (plan_resident(pr, st, c, rl, ri)) cands.push_back({c == 1 ? QPE_STRATEGY_RESIDENT : QPE_STRATEGY_CLUSTER, c});
-  if (cands.empty()) {
+  cands.push_back({QPE_STRATEGY_TILED, 0});
+  if (cands.size() == 1) {
     strategy = QPE_STRATEGY_TILED;
-  } else if (cands.size() == 1) {
-    strategy = cands[0].first;
-    K = cands[0].second;
   } else {
     cudaEvent_t e0, e1;
     QPE_CK(cudaEventCreate(&e0));
@@ -329,10 +351,14 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     float best = 1e30f;
     for (auto& c : cands) {
       float ms = 0;
+      auto run = [&]() {
+        if (c.first == QPE_STRATEGY_TILED) evolve_tiled(st, pr, 1, 2, exact);
+        else run_resident(st, pr, c.second, 1, 2, exact);
+      };
       try {
-        run_resident(st, pr, c.second, 1, 2);  // warm-up of this configuration
+        run();  // warm-up of this configuration
         QPE_CK(cudaEventRecord(e0, st->ctx->stream));
-        run_resident(st, pr, c.second, 1, 2);
+        run();
         QPE_CK(cudaEventRecord(e1, st->ctx->stream));
         QPE_CK(cudaEventSynchronize(e1));
         QPE_CK(cudaEventElapsedTime(&ms, e0, e1));
@@ -354,6 +380,7 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     cudaEventDestroy(e1);
   }
   st->tuned_prog = pr->id;
+  st->tuned_exact = exact;
   st->tuned_strategy = strategy;
   st->tuned_cluster = K;
 }
@@ -370,19 +397,20 @@ static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* 
   if (first < 1 || last > st->N || first > last) throw Error(QPE_ERR_INVALID, "power range outside 1 .. 2^P");
   st->probs_valid = false;
   if (first == last) return;
+  const bool exact = st->dtype == QPE_C128 && !(opts && (opts->flags & QPE_EVOLVE_FP64_CONTRACT));
   uint32_t strategy = 0, K = 0;
-  choose_strategy(st, pr, opts, strategy, K);
+  choose_strategy(st, pr, opts, exact, strategy, K);
   if (strategy == QPE_STRATEGY_TILED) {
-    evolve_tiled(st, pr, first, last);
+    evolve_tiled(st, pr, first, last, exact);
   } else {
-    run_resident(st, pr, K, first, last);
+    run_resident(st, pr, K, first, last, exact);
     QPE_CK(cudaStreamSynchronize(st->ctx->stream));
   }
 }
 
 // Global-memory working block, one kernel launch per pass, one captured graph
 // per controlled power replayed for every power.
-static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last) {
+static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last, bool exact) {
   const HostProgram& hp = pr->hp;
   cudaStream_t s = st->ctx->stream;
   if (!st->work.p) st->work.alloc(st->ld * st->esz);
@@ -391,17 +419,23 @@ static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, u
                          st->ld * st->esz, cudaMemcpyDeviceToDevice, s));
   k_set_int<<<1, 1, 0, s>>>(st->dk.as<int>(), (int)first);
   QPE_CK(cudaGetLastError());
-  if (st->graph_prog != pr->id || !st->graph) {
+  if (st->graph_prog != pr->id || st->graph_exact != (uint32_t)exact || !st->graph) {
     if (st->graph) cudaGraphExecDestroy(st->graph);
     st->graph = nullptr;
     st->graph_prog = 0;
     std::vector<PassLaunch> plans;
     size_t max_smem = 0;
-    for (const Pass& pass : hp.passes) {
-      plans.push_back(plan_pass(pr, st, pass));
-      const PassLaunch& pl = plans.back();
-      size_t sm = pass_stage_elems(pass, pl.Ca, pl.Cb, pl.W) * st->esz * pl.warps_per_cta;
-      if (sm > max_smem) max_smem = sm;
+    for (uint32_t sw = 0; sw < hp.steps * hp.order; ++sw) {
+      const bool rev = hp.order == 2 && (sw & 1);
+      for (size_t pj = 0; pj < hp.passes.size(); ++pj) {
+        const Pass& pass = hp.passes[rev ? hp.passes.size() - 1 - pj : pj];
+        plans.push_back(plan_pass(pr, st, pass));
+        PassLaunch& pl = plans.back();
+        pl.rev = rev ? 1u : 0u;
+        pl.exact = exact ? 1u : 0u;
+        size_t sm = pass_stage_elems(pass, pl.Ca, pl.Cb, pl.W) * st->esz * pl.warps_per_cta;
+        if (sm > max_smem) max_smem = sm;
+      }
     }
     QPE_CK(configure_pass_kernels(st->dtype, max_smem < 48 * 1024 ? 48 * 1024 : max_smem));
     cudaGraph_t g = nullptr;
@@ -423,6 +457,7 @@ static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, u
     QPE_CK(ie);
     st->graph = ge;
     st->graph_prog = pr->id;
+    st->graph_exact = exact;
   }
   for (uint32_t k = first; k < last; ++k) QPE_CK(cudaGraphLaunch(st->graph, s));
   QPE_CK(cudaStreamSynchronize(s));
@@ -736,13 +771,13 @@ static void fill_info(const HostProgram& hp, qpe_program_info* info) {
   info->c_alpha = (uint32_t)hp.Ca;
   info->c_beta = (uint32_t)hp.Cb;
   info->num_ops = hp.ops_per_sweep;
-  info->num_ops_per_power = (uint32_t)hp.ops.size();
+  info->num_ops_per_power = (uint32_t)(hp.ops.size() * hp.steps * hp.order);
   info->touches_per_sweep = hp.touches_per_sweep;
   info->touches_per_power = hp.touches_per_power;
   uint64_t entries = 0;
   for (const AxisTable& t : hp.tables) entries += t.count;
   info->table_entries = entries;
-  info->num_passes_per_power = (uint32_t)hp.passes.size();
+  info->num_passes_per_power = (uint32_t)(hp.passes.size() * hp.steps * hp.order);
   info->reserved = 0;
 }
 
@@ -824,6 +859,7 @@ int qpe_evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts
     if (opts && opts->strategy > QPE_STRATEGY_TILED) throw Error(QPE_ERR_INVALID, "unknown strategy");
     if (opts && opts->cluster_size && (opts->cluster_size > 16 || (opts->cluster_size & (opts->cluster_size - 1))))
       throw Error(QPE_ERR_INVALID, "cluster_size must be a power of two <= 16");
+    if (opts && (opts->flags & ~QPE_EVOLVE_FP64_CONTRACT)) throw Error(QPE_ERR_INVALID, "unknown evolve flag");
     evolve(st, pr, opts);
   });
 }

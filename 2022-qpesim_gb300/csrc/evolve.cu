@@ -66,7 +66,7 @@ __global__ void k_pass(PassLaunch pl) {
     }
     __syncwarp();
     if (PT == PASS_MIX) {
-      run_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, lane, 32, true, parb,
+      run_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, lane, 32, true, parb,
                         [&](uint32_t a) -> C2& { return st[2 * a]; },
                         [&](uint32_t a) -> C2& { return st[2 * a + 1]; });
     } else {
@@ -75,7 +75,8 @@ __global__ void k_pass(PassLaunch pl) {
       const bool active = w < nl;
       const uint32_t line = (PT == PASS_COL) ? b0 + w : row;
       const uint32_t lstr = active ? __ldg(((PT == PASS_COL) ? pl.strB : pl.strA) + line) : 0u;
-      run_line_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, L, lane >> logW, 32 >> logW, active, lstr,
+      run_line_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, L, lane >> logW, 32 >> logW,
+                         active, lstr,
                          [&](uint32_t e) -> C2& { return st[(e << logW) + w]; });
     }
     for (uint32_t i = lane; i < L * W; i += 32) {

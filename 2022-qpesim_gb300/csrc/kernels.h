@@ -40,6 +40,7 @@ struct PassLaunch {
   uint32_t warps_per_cta;
   uint32_t grid;
   uint32_t exact;             // complex128: reference rounding (no contraction)
+  uint32_t rev;               // run the pass's terms in reverse order
 };
 size_t pass_stage_elems(const Pass& pass, uint32_t Ca, uint32_t Cb, uint32_t W);
 cudaError_t launch_pass(const PassLaunch& pl, int dtype, cudaStream_t s);
@@ -63,6 +64,7 @@ struct ResidentInstance {
   uint32_t first, last;     // powers evolved: blocks first .. last - 1
   uint32_t rows_per_cta;    // rows owned by each CTA of the cluster
   uint32_t Wc, Wr, Wm;
+  uint32_t steps, order;    // Trotter steps per power; 2 = forward + backward sweep
 };
 struct ResidentLaunch {
   const ResidentInstance* insts;  // device array, ninst entries
@@ -73,6 +75,8 @@ struct ResidentLaunch {
   size_t smem_bytes;
 };
 cudaError_t launch_resident(const ResidentLaunch& rl, int dtype, int exact, cudaStream_t s);
+// Shared-memory carveout (percent of the maximum) the resident kernel asks for.
+cudaError_t set_resident_carveout(int dtype, int exact, int percent);
 cudaError_t resident_max_cluster(int dtype, uint32_t cluster, uint32_t warps, size_t smem, int* max_clusters);
 
 // ---- QIFT and reductions (qift.cu) ----

@@ -41,20 +41,28 @@ struct AxisTable {
   uint32_t offset;  // first word in the pool
 };
 
-enum OpKind : uint8_t { OPK_PAIR = 0, OPK_DIAG_LIST = 1, OPK_DIAG_ALL = 2 };
-
 // One term application inside a pass. `cond` bits (ncond of them) must all be
 // occupied in the line's own string for the term to act on that line (e.g. the
 // spectator q of a pqqr ABBA term, or the beta orbitals of a diagonal term
-// applied in a column pass).
-struct DevOp {
+// applied in a column pass). The coefficients are inline: for a pair term with a
+// real m00 = c0 and an imaginary m01 = i * c1 for parity 0 and -i * c1 for parity 1
+// (every term of the reference's getters: cos and -sin of h t), `c0`, `c1`; for a
+// diagonal term its complex coefficient (c0, c1). Any other pair matrix keeps its
+// 8-double record (even m00, m01, odd m00, m01) at index `gen` of the program's
+// coefficient array; gen == OP_INLINE marks the inline form.
+constexpr uint32_t OP_INLINE = 0xffffffffu;
+struct alignas(16) DevOp {
   uint32_t tab;    // word offset of the table (unused for OPK_DIAG_ALL)
   uint32_t count;  // table entries (OPK_DIAG_ALL: line length)
   uint8_t kind;
   uint8_t ncond;
   uint8_t cb0, cb1;
-  uint32_t coef;   // coefficient record (8 doubles: even m00, m01, odd m00, m01)
+  uint32_t gen;    // OP_INLINE, or the coefficient record of a general pair matrix
+  double c0, c1;
 };
+static_assert(sizeof(DevOp) == 32, "DevOp layout");
+
+enum OpKind : uint8_t { OPK_PAIR = 0, OPK_DIAG_LIST = 1, OPK_DIAG_ALL = 2 };
 
 enum PassType : uint8_t { PASS_COL = 0, PASS_ROW = 1, PASS_MIX = 2 };
 

@@ -185,7 +185,20 @@ struct Builder {
 
   DevOp encode(const AbsOp& a, uint32_t pass_type) {
     DevOp d{};
-    d.coef = a.coef;
+    const double* rec = &P.coefs[8 * (size_t)a.coef];
+    if (a.cls == 'D') {
+      d.gen = OP_INLINE;
+      d.c0 = rec[0];
+      d.c1 = rec[1];
+    } else if (rec[1] == 0.0 && rec[2] == 0.0 && rec[5] == 0.0 && rec[6] == 0.0 && rec[4] == rec[0] &&
+               rec[7] == -rec[3]) {
+      // m00 = (c, 0) for both parities, m01 = (0, t) for parity 0 and (0, -t) for 1
+      d.gen = OP_INLINE;
+      d.c0 = rec[0];
+      d.c1 = rec[3];
+    } else {
+      d.gen = a.coef;
+    }
     auto tab_ref = [&](int id) {
       d.tab = P.tables[id].offset;
       d.count = P.tables[id].count;
@@ -299,14 +312,12 @@ void build_program(HostProgram& P, unsigned M, unsigned na, unsigned nb, const T
 
   P.ops_per_sweep = (uint32_t)sweep.size();
   for (const AbsOp& a : sweep) P.touches_per_sweep += a.touches;
-
-  std::vector<AbsOp> power;
-  for (unsigned st = 0; st < steps; ++st) {
-    power.insert(power.end(), sweep.begin(), sweep.end());
-    if (order == 2) power.insert(power.end(), sweep.rbegin(), sweep.rend());
-  }
+  // One forward sweep is stored. A controlled power runs it `steps` times; a
+  // second-order step runs it forward and then backward (the passes in reverse
+  // order, each pass's terms in reverse order): segmenting the reversed term
+  // list gives the same passes reversed, so the backward sweep needs no copy.
   P.touches_per_power = P.touches_per_sweep * steps * order;
-  B.segment(power);
+  B.segment(sweep);
   if (P.pool_words == 0) P.pool_words = 1;
 }
 

@@ -24,9 +24,9 @@ struct HostProgram {
   unsigned order = 1, steps = 1;
   std::vector<AxisTable> tables;
   uint64_t pool_words = 0;
-  std::vector<DevOp> ops;      // one controlled power (steps x sweeps)
-  std::vector<double> coefs;   // 8 doubles per term record
-  std::vector<Pass> passes;    // one controlled power
+  std::vector<DevOp> ops;      // one forward Trotter sweep
+  std::vector<double> coefs;   // 8 doubles per term record (general matrices)
+  std::vector<Pass> passes;    // one forward Trotter sweep
   uint32_t ops_per_sweep = 0;
   uint64_t touches_per_sweep = 0;
   uint64_t touches_per_power = 0;

@@ -67,8 +67,14 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
   }
   barrier();
 
+  const uint32_t nsweeps = I.steps * I.order;
   for (uint32_t k = I.first; k < I.last; ++k) {
-    for (uint32_t pi = 0; pi < I.npasses; ++pi) {
+    for (uint32_t sw = 0; sw < nsweeps; ++sw) {
+    // Second-order steps alternate a forward and a backward sweep; the backward
+    // sweep runs the passes, and each pass's terms, in reverse order.
+    const bool rev = I.order == 2 && (sw & 1);
+    for (uint32_t pj = 0; pj < I.npasses; ++pj) {
+      const uint32_t pi = rev ? I.npasses - 1 - pj : pj;
       const Pass P = I.passes[pi];
       if (P.type == PASS_ROW) {
         // Rows owned by this CTA, Wr rows per warp tile, in place.
@@ -80,7 +86,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
           const bool active = r < row1;
           const uint32_t lstr = active ? __ldg(I.strA + r) : 0u;
           C2* line = blk + (size_t)(active ? r - row0 : 0) * Cb;
-          run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, Cb, jl, jstep, active, lstr,
+          run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, Cb, jl, jstep, active, lstr,
                              [&](uint32_t e) -> C2& { return line[e]; });
         }
       } else if (P.type == PASS_COL) {
@@ -94,7 +100,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
           const uint32_t lstr = active ? __ldg(I.strB + c) : 0u;
           if (K == 1) {
             C2* col = blk + (active ? c : 0);
-            run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, Ca, jl, jstep, active, lstr,
+            run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, Ca, jl, jstep, active, lstr,
                                [&](uint32_t e) -> C2& { return col[(size_t)e * Cb]; });
           } else {
             const uint32_t nl = min(W, Cb - b0);
@@ -103,7 +109,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
               if (ww < nl) stage[i] = *at(e, b0 + ww);
             }
             __syncwarp();
-            run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, Ca, jl, jstep, active, lstr,
+            run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, Ca, jl, jstep, active, lstr,
                                [&](uint32_t e) -> C2& { return stage[(e << logW) + w]; });
             for (uint32_t i = lane; i < (Ca << logW); i += 32) {
               const uint32_t e = i >> logW, ww = i & (W - 1);
@@ -124,7 +130,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
           const uint2 bp = active ? __ldg(mt + t) : make_uint2(0u, 0u);
           const uint32_t b01 = bp.x & 0x7fffffffu, b10 = bp.y, parb = bp.x >> 31;
           if (K == 1) {
-            run_mix_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, jl, jstep, active, parb,
+            run_mix_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, jl, jstep, active, parb,
                               [&](uint32_t a) -> C2& { return blk[(size_t)a * Cb + b01]; },
                               [&](uint32_t a) -> C2& { return blk[(size_t)a * Cb + b10]; });
           } else {
@@ -138,7 +144,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
               }
             }
             __syncwarp();
-            run_mix_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, jl, jstep, active, parb,
+            run_mix_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, jl, jstep, active, parb,
                               [&](uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w]; },
                               [&](uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w + 1]; });
             for (uint32_t i = lane; i < n2; i += 32) {
@@ -153,6 +159,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
         }
       }
       barrier();
+    }
     }
     // Snapshot of this CTA's rows into block k.
     C2* dst = gstate + (uint64_t)k * ld + (uint64_t)row0 * Cb;
@@ -192,6 +199,16 @@ cudaError_t launch_resident(const ResidentLaunch& rl, int dtype, int exact, cuda
     return launch_res<double, Fast<double>>(rl, s);
   }
   return launch_res<float, Fast<float>>(rl, s);
+}
+
+cudaError_t set_resident_carveout(int dtype, int exact, int percent) {
+  if (dtype == QPE_C128) {
+    if (exact)
+      return cudaFuncSetAttribute(k_resident<double, ExactD>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+    return cudaFuncSetAttribute(k_resident<double, Fast<double>>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                percent);
+  }
+  return cudaFuncSetAttribute(k_resident<float, Fast<float>>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
 }
 
 cudaError_t resident_max_cluster(int dtype, uint32_t cluster, uint32_t warps, size_t smem, int* max_clusters) {

@@ -50,17 +50,44 @@ struct Coef4 {
   bool reduced;  // m00 real and m01 imaginary for both parities
 };
 
+// A term's descriptor with its coefficients in registers.
 template <typename R>
-__device__ __forceinline__ Coef4<R> load_coef(const double* __restrict__ c) {
+struct OpR {
+  DevOp d;
   Coef4<R> k;
-  const double2 a = __ldg(reinterpret_cast<const double2*>(c));
-  const double2 b = __ldg(reinterpret_cast<const double2*>(c) + 1);
-  const double2 d = __ldg(reinterpret_cast<const double2*>(c) + 2);
-  const double2 e = __ldg(reinterpret_cast<const double2*>(c) + 3);
-  k.e0r = (R)a.x; k.e0i = (R)a.y; k.e1r = (R)b.x; k.e1i = (R)b.y;
-  k.o0r = (R)d.x; k.o0i = (R)d.y; k.o1r = (R)e.x; k.o1i = (R)e.y;
-  k.reduced = a.y == 0.0 && b.x == 0.0 && d.y == 0.0 && e.x == 0.0;
-  return k;
+};
+
+template <typename R>
+__device__ __forceinline__ OpR<R> load_op(const DevOp* __restrict__ ops, const double* __restrict__ coef, uint32_t o) {
+  OpR<R> r;
+  const uint4* src = reinterpret_cast<const uint4*>(ops + o);
+  const uint4 a = __ldg(src), b = __ldg(src + 1);
+  r.d.tab = a.x;
+  r.d.count = a.y;
+  r.d.kind = (uint8_t)(a.z & 0xff);
+  r.d.ncond = (uint8_t)((a.z >> 8) & 0xff);
+  r.d.cb0 = (uint8_t)((a.z >> 16) & 0xff);
+  r.d.cb1 = (uint8_t)(a.z >> 24);
+  r.d.gen = a.w;
+  r.d.c0 = __hiloint2double((int)b.y, (int)b.x);
+  r.d.c1 = __hiloint2double((int)b.w, (int)b.z);
+  if (r.d.gen == OP_INLINE) {
+    // diagonal (c0, c1); pair m00 = c0, m01 = i c1 (parity 0) / -i c1 (parity 1)
+    r.k.e0r = r.k.o0r = (R)r.d.c0;
+    r.k.e0i = r.k.o0i = (R)0;
+    r.k.e1r = r.k.o1r = (R)0;
+    r.k.e1i = (R)r.d.c1;
+    r.k.o1i = -(R)r.d.c1;
+    r.k.reduced = r.d.kind == OPK_PAIR;
+    if (r.d.kind != OPK_PAIR) r.k.e0i = (R)r.d.c1;
+  } else {
+    const double2* c = reinterpret_cast<const double2*>(coef + 8 * (size_t)r.d.gen);
+    const double2 x0 = __ldg(c), x1 = __ldg(c + 1), x2 = __ldg(c + 2), x3 = __ldg(c + 3);
+    r.k.e0r = (R)x0.x; r.k.e0i = (R)x0.y; r.k.e1r = (R)x1.x; r.k.e1i = (R)x1.y;
+    r.k.o0r = (R)x2.x; r.k.o0i = (R)x2.y; r.k.o1r = (R)x3.x; r.k.o1i = (R)x3.y;
+    r.k.reduced = false;
+  }
+  return r;
 }
 
 template <class A, typename R>
@@ -111,96 +138,94 @@ __device__ __forceinline__ bool cond_ok(uint32_t line_str, const DevOp& op) {
   return (line_str & m) == m;
 }
 
-// Runs the terms [op0, op1) of a COL or ROW pass on this lane's line. `elem(e)`
-// returns a reference to entry e of the line; `active` is false for lanes past
-// the last line; `lstr` is the line's occupation string (for conditions).
-// The loop is software-pipelined: the next term's descriptor, coefficients and
-// this lane's first table entry are loaded while the current term computes, so
-// the chain of dependent terms pays the shared-memory latency, not the latency
-// of the metadata loads.
+// Runs the terms [op0, op1) of a COL or ROW pass on this lane's line, in order,
+// or in reverse order when `rev` (the backward half of a second-order step).
+// `elem(e)` returns a reference to entry e of the line; `active` is false for
+// lanes past the last line; `lstr` is the line's occupation string (for
+// conditions). The loop is software-pipelined: the next term's descriptor,
+// coefficients and this lane's first table entry are loaded while the current
+// term computes, so the chain of dependent terms pays shared-memory latency
+// rather than the latency of the metadata loads.
 template <typename R, class A, class Elem>
 __device__ __forceinline__ void run_line_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
-                                             const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1,
+                                             const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1, bool rev,
                                              uint32_t L, uint32_t jl, uint32_t jstep, bool active, uint32_t lstr,
                                              Elem elem) {
-  if (op0 >= op1) return;
+  const uint32_t n = op1 - op0;
+  if (n == 0) return;
+  auto at = [&](uint32_t i) { return rev ? op1 - 1 - i : op0 + i; };
   auto first_of = [&](const DevOp& d) -> uint2 {
     return (d.kind == OPK_PAIR && jl < d.count) ? __ldg(reinterpret_cast<const uint2*>(pool + d.tab) + jl)
                                                 : make_uint2(0u, 0u);
   };
-  DevOp op = ops[op0];
-  Coef4<R> k = load_coef<R>(coef + 8 * (size_t)op.coef);
-  uint2 first = first_of(op);
-  for (uint32_t o = op0; o < op1; ++o) {
-    DevOp opn = op;
-    Coef4<R> kn = k;
+  OpR<R> op = load_op<R>(ops, coef, at(0));
+  uint2 first = first_of(op.d);
+  for (uint32_t i = 0; i < n; ++i) {
+    OpR<R> opn = op;
     uint2 firstn = make_uint2(0u, 0u);
-    if (o + 1 < op1) {
-      opn = ops[o + 1];
-      kn = load_coef<R>(coef + 8 * (size_t)opn.coef);
-      firstn = first_of(opn);
+    if (i + 1 < n) {
+      opn = load_op<R>(ops, coef, at(i + 1));
+      firstn = first_of(opn.d);
     }
-    if (active && (op.ncond == 0 || cond_ok(lstr, op))) {
-      if (op.kind == OPK_PAIR) {
-        const uint2* __restrict__ t = reinterpret_cast<const uint2*>(pool + op.tab);
+    const DevOp& d = op.d;
+    if (active && (d.ncond == 0 || cond_ok(lstr, d))) {
+      if (d.kind == OPK_PAIR) {
+        const uint2* __restrict__ t = reinterpret_cast<const uint2*>(pool + d.tab);
         uint2 x = first;
-        for (uint32_t j = jl; j < op.count; j += jstep) {
+        for (uint32_t j = jl; j < d.count; j += jstep) {
           const uint32_t jn = j + jstep;
-          const uint2 xn = jn < op.count ? __ldg(t + jn) : make_uint2(0u, 0u);
-          pair_update<A>(elem(x.x & 0x7fffffffu), elem(x.y), k, x.x >> 31);
+          const uint2 xn = jn < d.count ? __ldg(t + jn) : make_uint2(0u, 0u);
+          pair_update<A>(elem(x.x & 0x7fffffffu), elem(x.y), op.k, x.x >> 31);
           x = xn;
         }
-      } else if (op.kind == OPK_DIAG_LIST) {
-        for (uint32_t j = jl; j < op.count; j += jstep) diag_update<A>(elem(__ldg(pool + op.tab + j)), k);
+      } else if (d.kind == OPK_DIAG_LIST) {
+        for (uint32_t j = jl; j < d.count; j += jstep) diag_update<A>(elem(__ldg(pool + d.tab + j)), op.k);
       } else {
-        for (uint32_t e = jl; e < L; e += jstep) diag_update<A>(elem(e), k);
+        for (uint32_t e = jl; e < L; e += jstep) diag_update<A>(elem(e), op.k);
       }
     }
     __syncwarp();
     op = opn;
-    k = kn;
     first = firstn;
   }
 }
 
-// Runs the pqrs ABBA terms [op0, op1) of a MIX pass on this lane's column pair:
-// entry (a01 | par, a10) pairs left(a01) with right(a10), parity adding the beta
-// pair's parity parb (cpp/time_evolution_over_terms.hpp:774). Pipelined as
-// run_line_ops.
+// Runs the pqrs ABBA terms [op0, op1) of a MIX pass on this lane's column pair
+// (reverse order when `rev`): entry (a01 | par, a10) pairs left(a01) with
+// right(a10), parity adding the beta pair's parity parb
+// (cpp/time_evolution_over_terms.hpp:774). Pipelined as run_line_ops.
 template <typename R, class A, class Left, class Right>
 __device__ __forceinline__ void run_mix_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
-                                            const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1,
+                                            const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1, bool rev,
                                             uint32_t jl, uint32_t jstep, bool active, uint32_t parb, Left left,
                                             Right right) {
-  if (op0 >= op1) return;
+  const uint32_t n = op1 - op0;
+  if (n == 0) return;
+  auto at = [&](uint32_t i) { return rev ? op1 - 1 - i : op0 + i; };
   auto first_of = [&](const DevOp& d) -> uint2 {
     return jl < d.count ? __ldg(reinterpret_cast<const uint2*>(pool + d.tab) + jl) : make_uint2(0u, 0u);
   };
-  DevOp op = ops[op0];
-  Coef4<R> k = load_coef<R>(coef + 8 * (size_t)op.coef);
-  uint2 first = first_of(op);
-  for (uint32_t o = op0; o < op1; ++o) {
-    DevOp opn = op;
-    Coef4<R> kn = k;
+  OpR<R> op = load_op<R>(ops, coef, at(0));
+  uint2 first = first_of(op.d);
+  for (uint32_t i = 0; i < n; ++i) {
+    OpR<R> opn = op;
     uint2 firstn = make_uint2(0u, 0u);
-    if (o + 1 < op1) {
-      opn = ops[o + 1];
-      kn = load_coef<R>(coef + 8 * (size_t)opn.coef);
-      firstn = first_of(opn);
+    if (i + 1 < n) {
+      opn = load_op<R>(ops, coef, at(i + 1));
+      firstn = first_of(opn.d);
     }
-    const uint2* __restrict__ t = reinterpret_cast<const uint2*>(pool + op.tab);
-    uint2 x = first;
     if (active) {
-      for (uint32_t j = jl; j < op.count; j += jstep) {
+      const uint2* __restrict__ t = reinterpret_cast<const uint2*>(pool + op.d.tab);
+      uint2 x = first;
+      for (uint32_t j = jl; j < op.d.count; j += jstep) {
         const uint32_t jn = j + jstep;
-        const uint2 xn = jn < op.count ? __ldg(t + jn) : make_uint2(0u, 0u);
-        pair_update<A>(left(x.x & 0x7fffffffu), right(x.y), k, (x.x >> 31) ^ parb);
+        const uint2 xn = jn < op.d.count ? __ldg(t + jn) : make_uint2(0u, 0u);
+        pair_update<A>(left(x.x & 0x7fffffffu), right(x.y), op.k, (x.x >> 31) ^ parb);
         x = xn;
       }
     }
     __syncwarp();
     op = opn;
-    k = kn;
     first = firstn;
   }
 }

@@ -120,11 +120,12 @@ class DeviceState:
         N.check(self._lib.qpe_state_zero(self._h))
 
     def evolve(self, program: Program, first_power: int = 0, last_power: int = 0, strategy: int = 0,
-               cluster_size: int = 0) -> None:
+               cluster_size: int = 0, fp64_contract: bool = False) -> None:
         """strategy: 0 auto (autotuned per program), 1 one CTA resident in shared
         memory, 2 a cluster of cluster_size CTAs (0: smallest that fits), 3
-        global-memory tile passes."""
-        opts = N.EvolveOpts(strategy, first_power, last_power, cluster_size)
+        global-memory tile passes. fp64_contract allows FMAs in complex128
+        (within 1e-12 of the reference instead of bit-identical)."""
+        opts = N.EvolveOpts(strategy, first_power, last_power, cluster_size, 1 if fp64_contract else 0)
         N.check(self._lib.qpe_evolve(self._h, program._h, C.byref(opts)))
 
     def qift(self) -> None:

@@ -191,11 +191,17 @@ int qpe_state_zero(qpe_state* st);
 #define QPE_STRATEGY_CLUSTER 2  /* block spread over a thread-block cluster */
 #define QPE_STRATEGY_TILED 3    /* L2-resident block, shared-memory tile passes */
 
+/* complex128 only: allow fused multiply-adds. Results then differ from the
+ * reference's rounding by a few ulps per update (within 1e-12 of it) instead of
+ * being bit-identical, for about a third fewer FP64 instructions. */
+#define QPE_EVOLVE_FP64_CONTRACT 1u
+
 typedef struct qpe_evolve_opts {
   uint32_t strategy;     /* QPE_STRATEGY_* */
   uint32_t first_power;  /* evolve blocks first_power .. last_power - 1 (0, 0 = all) */
   uint32_t last_power;
   uint32_t cluster_size; /* QPE_STRATEGY_CLUSTER: CTAs per cluster (0 = auto) */
+  uint32_t flags;        /* QPE_EVOLVE_* */
 } qpe_evolve_opts;
 
 /* block_k <- U * block_{k-1} for k = 1 .. 2^P - 1 on the device (opts may be NULL). */

