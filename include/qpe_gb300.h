@@ -213,6 +213,27 @@ int qpe_state_phase_probs(qpe_state* st, double* probs);
 /* Per-block squared norms (2^P doubles, FP64 accumulation). */
 int qpe_state_block_norms(qpe_state* st, double* norms);
 
+/* ---- QIFT without any allocation ------------------------------------------------
+ * No counterpart in the reference. For callers that cannot allocate device memory
+ * when they need the QIFT: code whose stream is being captured into a CUDA graph
+ * (cudaMalloc is not allowed during capture), or a host that hands out all device
+ * memory from its own pool. Runs the QIFT of qpe_state_qift in place on the
+ * caller's device register d_state (2^precision x ld elements of dtype) on the
+ * caller's cudaStream_t `stream` and writes the phase histogram (2^precision
+ * doubles) to the device buffer d_probs. It calls no allocator: the kernel's
+ * scratch (histogram partial rows and twiddles) is one fixed array of
+ * QPE_NOALLOC_SCRATCH_DOUBLES doubles (about 2 MiB) inside the library, which
+ * every GPU that loads the library holds until the process exits; precision
+ * above QPE_NOALLOC_MAX_PRECISION is rejected with QPE_ERR_UNSUPPORTED. The first
+ * call on a device sets up the array's device address (cudaGetSymbolAddress), so
+ * make it before any stream capture. All calls share the array: calls that
+ * overlap on the GPU (other streams, other host threads) race on it. */
+#define QPE_NOALLOC_MAX_PRECISION 10
+#define QPE_NOALLOC_MAX_CTAS 256
+#define QPE_NOALLOC_SCRATCH_DOUBLES ((QPE_NOALLOC_MAX_CTAS << QPE_NOALLOC_MAX_PRECISION) + (1 << QPE_NOALLOC_MAX_PRECISION))
+int qpe_qift_device_noalloc(void* stream, uint32_t precision, uint64_t ld, int dtype, void* d_state,
+                            double* d_probs);
+
 #ifdef __cplusplus
 }
 #endif
