@@ -10,6 +10,7 @@ The directory is named 2022-qpesim_gb300, which is not an importable module
 name; __graft_entry__.load_package() registers it as `qpesim_gb300`.
 """
 from . import _native
+from .batching import Batch
 from .hamiltonian import Hamiltonian, SpinIndex
 from .offset_computer import OffsetComputer
 from .readout import (argmax_phase, margin_of_error, phase_to_energy, reference_energy, reference_phase,
@@ -22,7 +23,7 @@ QpeError = _native.QpeError
 TERM_DTYPE = _native.TERM_DTYPE
 LIB_PATH = _native.LIB_PATH
 
-__all__ = ["Hamiltonian", "SpinIndex", "OffsetComputer", "StateVector", "time_evolve_over_terms", "Program",
+__all__ = ["Batch", "Hamiltonian", "SpinIndex", "OffsetComputer", "StateVector", "time_evolve_over_terms", "Program",
            "DeviceState", "plan_program", "Integrals", "synthetic_integrals", "hf_block0", "QpeError", "TERM_DTYPE",
            "reference_phase", "reference_energy", "margin_of_error", "phase_to_energy", "argmax_phase",
            "subbin_phase", "success_probability"]

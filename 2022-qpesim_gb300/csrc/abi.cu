@@ -8,73 +8,19 @@
 #include <string>
 #include <vector>
 
-#include "../../include/qpe_gb300.h"
-#include "kernels.h"
-#include "program_build.h"
-#include "qpe_common.h"
+#include "abi_internal.h"
 
 namespace qpe {
 
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
-
-#define QPE_CK(expr)                                                                              \
-  do {                                                                                            \
-    cudaError_t e_ = (expr);                                                                      \
-    if (e_ != cudaSuccess)                                                                        \
-      throw ::qpe::Error(e_ == cudaErrorNoDevice || e_ == cudaErrorInsufficientDriver             \
-                             ? QPE_ERR_NO_DEVICE                                                  \
-                             : (e_ == cudaErrorMemoryAllocation ? QPE_ERR_NOMEM : QPE_ERR_CUDA),  \
-                         std::string(#expr) + ": " + cudaGetErrorString(e_));                     \
-  } while (0)
-
-// Device buffer with RAII release.
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  DevBuf() = default;
-  DevBuf(const DevBuf&) = delete;
-  DevBuf& operator=(const DevBuf&) = delete;
-  ~DevBuf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-  void alloc(size_t n) {
-    release();
-    if (n == 0) n = 16;
-    QPE_CK(cudaMalloc(&p, n));
-    bytes = n;
-  }
-  template <class T>
-  T* as() const {
-    return reinterpret_cast<T*>(p);
-  }
-};
+const std::string& last_error_message() { return g_last_error; }
 
 __global__ void k_set_int(int* p, int v) { *p = v; }
 
 }  // namespace qpe
 
 using namespace qpe;
-
-struct qpe_context {
-  int device = 0;
-  int num_sms = 0;
-  size_t smem_optin = 0;
-  cudaStream_t stream = nullptr;
-  DevBuf binom;
-  DevBuf flush;
-  cudaEvent_t events[16] = {};
-};
-
-struct qpe_program {
-  qpe_context* ctx = nullptr;
-  uint64_t id = 0;  // unique per process, keys the cached evolution graphs
-  HostProgram hp;
-  DevBuf pool, ops, coef, strA, strB, tabs, start, passes;
-};
 
 struct qpe_state {
   qpe_context* ctx = nullptr;
@@ -108,6 +54,39 @@ static void check_ctx(qpe_context* ctx) {
   use_device(ctx);
 }
 
+void qift_geometry(uint32_t P, uint64_t ld, int dtype, int num_sms, size_t smem_optin, uint32_t& T, uint32_t& grid) {
+  const size_t esz = dtype == QPE_C128 ? 16 : 8;
+  const size_t row_bytes = ((size_t)1 << P) * esz;
+  if (row_bytes > smem_optin) throw Error(QPE_ERR_UNSUPPORTED, "precision too large for the QIFT tile");
+  T = 32;
+  while (T > 1 && (row_bytes * T > 96 * 1024 || T > ld)) T >>= 1;
+  uint64_t tiles = (ld + T - 1) / T;
+  uint64_t g = (uint64_t)num_sms * 2;
+  if (g > tiles) g = tiles;
+  grid = (uint32_t)g;
+}
+
+// Twiddles exp(-2 pi i k / N), k < N / 2, rounded from long double (as the oracle).
+void state_twiddles(uint32_t P, int dtype, DevBuf& tw) {
+  const uint64_t N = 1ull << P;
+  const uint64_t nh = N / 2 ? N / 2 : 1;
+  std::vector<double> twd(2 * nh);
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  for (uint64_t k = 0; k < nh; ++k) {
+    long double ang = -two_pi * (long double)k / (long double)N;
+    twd[2 * k] = (double)cosl(ang);
+    twd[2 * k + 1] = (double)sinl(ang);
+  }
+  if (dtype == QPE_C128) {
+    tw.alloc(twd.size() * sizeof(double));
+    QPE_CK(cudaMemcpy(tw.p, twd.data(), twd.size() * sizeof(double), cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> twf(twd.begin(), twd.end());
+    tw.alloc(twf.size() * sizeof(float));
+    QPE_CK(cudaMemcpy(tw.p, twf.data(), twf.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
+}
+
 static void state_alloc(qpe_state* st) {
   st->esz = st->dtype == QPE_C128 ? 16 : 8;
   st->N = 1ull << st->P;
@@ -115,36 +94,10 @@ static void state_alloc(qpe_state* st) {
   st->data.alloc(st->N * st->ld * st->esz);
   st->dk.alloc(sizeof(int));
   st->probs.alloc(st->N * sizeof(double));
-  // QIFT geometry: T columns per CTA, shared-memory tile N x T.
-  const size_t row_bytes = st->N * st->esz;
-  if (row_bytes > st->ctx->smem_optin) throw Error(QPE_ERR_UNSUPPORTED, "precision too large for the QIFT tile");
-  uint32_t T = 32;
-  while (T > 1 && (row_bytes * T > 96 * 1024 || T > st->ld)) T >>= 1;
-  st->qift_T = T;
-  uint64_t tiles = (st->ld + T - 1) / T;
-  uint64_t grid = (uint64_t)st->ctx->num_sms * 2;
-  if (grid > tiles) grid = tiles;
-  st->qift_grid = (uint32_t)grid;
-  st->partial.alloc(grid * st->N * sizeof(double));
-  // Twiddles exp(-2 pi i k / N), k < N / 2, rounded from long double (as the oracle).
-  const uint64_t nh = st->N / 2 ? st->N / 2 : 1;
-  std::vector<double> twd(2 * nh);
-  const long double two_pi = 6.283185307179586476925286766559005768L;
-  for (uint64_t k = 0; k < nh; ++k) {
-    long double ang = -two_pi * (long double)k / (long double)st->N;
-    twd[2 * k] = (double)cosl(ang);
-    twd[2 * k + 1] = (double)sinl(ang);
-  }
-  if (st->dtype == QPE_C128) {
-    st->tw.alloc(twd.size() * sizeof(double));
-    QPE_CK(cudaMemcpy(st->tw.p, twd.data(), twd.size() * sizeof(double), cudaMemcpyHostToDevice));
-  } else {
-    std::vector<float> twf(twd.begin(), twd.end());
-    st->tw.alloc(twf.size() * sizeof(float));
-    QPE_CK(cudaMemcpy(st->tw.p, twf.data(), twf.size() * sizeof(float), cudaMemcpyHostToDevice));
-  }
-  const size_t qsm = qift_smem_bytes(st->P, T, st->dtype);
-  QPE_CK(configure_qift_kernels(st->dtype, qsm));
+  qift_geometry(st->P, st->ld, st->dtype, st->ctx->num_sms, st->ctx->smem_optin, st->qift_T, st->qift_grid);
+  st->partial.alloc((size_t)st->qift_grid * st->N * sizeof(double));
+  state_twiddles(st->P, st->dtype, st->tw);
+  QPE_CK(configure_qift_kernels(st->dtype, qift_smem_bytes(st->P, st->qift_T, st->dtype)));
 }
 
 static void build_device_program(qpe_program* pr) {
@@ -184,11 +137,10 @@ static void build_device_program(qpe_program* pr) {
   QPE_CK(cudaStreamSynchronize(s));
 }
 
-// Launch geometry of one pass for a state of element size esz.
-static PassLaunch plan_pass(const qpe_program* pr, const qpe_state* st, const Pass& pass) {
+// Launch geometry of one pass for elements of esz bytes.
+PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_optin, const Pass& pass) {
   const HostProgram& hp = pr->hp;
   PassLaunch pl{};
-  pl.work = st->work.p;
   pl.pool = pr->pool.as<uint32_t>();
   pl.ops = pr->ops.as<DevOp>();
   pl.coef = pr->coef.as<double>();
@@ -197,8 +149,6 @@ static PassLaunch plan_pass(const qpe_program* pr, const qpe_state* st, const Pa
   pl.Ca = (uint32_t)hp.Ca;
   pl.Cb = (uint32_t)hp.Cb;
   pl.pass = pass;
-  pl.exact = st->dtype == QPE_C128 ? 1u : 0u;
-  const size_t esz = st->esz;
   const size_t warp_budget = 24 * 1024;
   uint32_t W = 1;
   if (pass.type == PASS_COL) {
@@ -206,16 +156,23 @@ static PassLaunch plan_pass(const qpe_program* pr, const qpe_state* st, const Pa
   }
   pl.W = W;
   const size_t stage = pass_stage_elems(pass, pl.Ca, pl.Cb, W) * esz;
-  if (stage > st->ctx->smem_optin) throw Error(QPE_ERR_UNSUPPORTED, "block too large for a shared-memory tile");
+  if (stage > smem_optin) throw Error(QPE_ERR_UNSUPPORTED, "block too large for a shared-memory tile");
   uint32_t wpc = 4;
-  while (wpc > 1 && stage * wpc > st->ctx->smem_optin) --wpc;
+  while (wpc > 1 && stage * wpc > smem_optin) --wpc;
   pl.warps_per_cta = wpc;
   uint64_t ntiles = pass.type == PASS_COL ? (hp.Cb + W - 1) / W : (pass.type == PASS_ROW ? hp.Ca : pass.mixcount);
   uint64_t grid = (ntiles + wpc - 1) / wpc;
-  const uint64_t cap = (uint64_t)st->ctx->num_sms * 8;
+  const uint64_t cap = (uint64_t)pr->ctx->num_sms * 8;
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
   pl.grid = (uint32_t)grid;
+  return pl;
+}
+
+static PassLaunch plan_pass(const qpe_program* pr, const qpe_state* st, const Pass& pass) {
+  PassLaunch pl = plan_pass_geometry(pr, st->esz, st->ctx->smem_optin, pass);
+  pl.work = st->work.p;
+  pl.exact = st->dtype == QPE_C128 ? 1u : 0u;
   return pl;
 }
 

@@ -1,0 +1,81 @@
+// abi_internal.h - the ABI's handle types and helpers, shared by the .cu files
+// that implement include/qpe_gb300.h.
+#ifndef QPE_ABI_INTERNAL_H_
+#define QPE_ABI_INTERNAL_H_
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/qpe_gb300.h"
+#include "kernels.h"
+#include "program_build.h"
+#include "qpe_common.h"
+
+namespace qpe {
+
+#define QPE_CK(expr)                                                                              \
+  do {                                                                                            \
+    cudaError_t e_ = (expr);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      throw ::qpe::Error(e_ == cudaErrorNoDevice || e_ == cudaErrorInsufficientDriver             \
+                             ? QPE_ERR_NO_DEVICE                                                  \
+                             : (e_ == cudaErrorMemoryAllocation ? QPE_ERR_NOMEM : QPE_ERR_CUDA),  \
+                         std::string(#expr) + ": " + cudaGetErrorString(e_));                     \
+  } while (0)
+
+// Device buffer with RAII release.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void alloc(size_t n) {
+    release();
+    if (n == 0) n = 16;
+    QPE_CK(cudaMalloc(&p, n));
+    bytes = n;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+const std::string& last_error_message();
+
+}  // namespace qpe
+
+struct qpe_context {
+  int device = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  qpe::DevBuf binom;
+  qpe::DevBuf flush;
+  cudaEvent_t events[16] = {};
+};
+
+struct qpe_program {
+  qpe_context* ctx = nullptr;
+  uint64_t id = 0;  // unique per process, keys the cached evolution graphs
+  qpe::HostProgram hp;
+  qpe::DevBuf pool, ops, coef, strA, strB, tabs, start, passes;
+};
+
+namespace qpe {
+// Launch geometry of one pass of `pr` for elements of esz bytes.
+PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_optin, const Pass& pass);
+void state_twiddles(uint32_t P, int dtype, DevBuf& tw);
+void qift_geometry(uint32_t P, uint64_t ld, int dtype, int num_sms, size_t smem_optin, uint32_t& T, uint32_t& grid);
+}  // namespace qpe
+
+#endif  // QPE_ABI_INTERNAL_H_

@@ -36,15 +36,18 @@ __global__ void k_pass(PassLaunch pl) {
   const uint32_t W = (PT == PASS_COL) ? pl.W : (PT == PASS_ROW ? 1u : 2u);
   const uint32_t L = (PT == PASS_ROW) ? Cb : Ca;
   const uint32_t logW = __ffs(W) - 1;
-  C2* __restrict__ blk = reinterpret_cast<C2*>(pl.work);
   C2* __restrict__ st = reinterpret_cast<C2*>(smem_raw) + (size_t)warp * L * W;
   const uint32_t* __restrict__ pool = pl.pool;
   uint32_t ntiles;
   if (PT == PASS_COL) ntiles = (Cb + W - 1) >> logW;
   else if (PT == PASS_ROW) ntiles = Ca;
   else ntiles = pl.pass.mixcount;
+  const uint32_t nmem = pl.nmem ? pl.nmem : 1u;
 
-  for (uint32_t tile = blockIdx.x * wpc + warp; tile < ntiles; tile += gridDim.x * wpc) {
+  for (uint32_t gt = blockIdx.x * wpc + warp; gt < ntiles * nmem; gt += gridDim.x * wpc) {
+    const uint32_t mem = gt / ntiles, tile = gt - mem * ntiles;
+    C2* __restrict__ blk = reinterpret_cast<C2*>(pl.works ? pl.works[mem] : pl.work);
+    const double2* icoef = pl.icoef ? pl.icoef + (size_t)mem * pl.nops : nullptr;
     uint32_t b0 = 0, b01 = 0, b10 = 0, parb = 0, row = 0;
     if (PT == PASS_COL) b0 = tile << logW;
     if (PT == PASS_ROW) row = tile;
@@ -68,7 +71,7 @@ __global__ void k_pass(PassLaunch pl) {
     if (PT == PASS_MIX) {
       run_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, lane, 32, true, parb,
                         [&](uint32_t a) -> C2& { return st[2 * a]; },
-                        [&](uint32_t a) -> C2& { return st[2 * a + 1]; });
+                        [&](uint32_t a) -> C2& { return st[2 * a + 1]; }, icoef);
     } else {
       // Lane l owns line l % W and walks entries l / W, l / W + 32 / W, ...
       const uint32_t w = lane & (W - 1);
@@ -76,8 +79,7 @@ __global__ void k_pass(PassLaunch pl) {
       const uint32_t line = (PT == PASS_COL) ? b0 + w : row;
       const uint32_t lstr = active ? __ldg(((PT == PASS_COL) ? pl.strB : pl.strA) + line) : 0u;
       run_line_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, L, lane >> logW, 32 >> logW,
-                         active, lstr,
-                         [&](uint32_t e) -> C2& { return st[(e << logW) + w]; });
+                         active, lstr, [&](uint32_t e) -> C2& { return st[(e << logW) + w]; }, icoef);
     }
     for (uint32_t i = lane; i < L * W; i += 32) {
       const uint32_t e = i >> logW, w = i & (W - 1);
@@ -150,6 +152,32 @@ __global__ void k_snapshot(const C2* __restrict__ work, C2* __restrict__ state, 
 
 __global__ void k_advance(int* d_k) { *d_k += 1; }
 
+template <typename C2>
+__global__ void k_snapshot_batch(void* const* __restrict__ works, void* const* __restrict__ states, uint64_t n,
+                                 const int* d_k, uint32_t nmem) {
+  const uint64_t k = (uint64_t)*d_k;
+  const uint64_t total = n * nmem;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t m = i / n, e = i - m * n;
+    reinterpret_cast<C2*>(states[m])[k * n + e] = reinterpret_cast<const C2*>(works[m])[e];
+  }
+}
+
+template <typename C2>
+__global__ void k_load_batch(void* const* __restrict__ works, void* const* __restrict__ states, uint64_t n,
+                             uint32_t block, uint32_t nmem) {
+  const uint64_t total = n * nmem;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t m = i / n, e = i - m * n;
+    reinterpret_cast<C2*>(works[m])[e] = reinterpret_cast<const C2*>(states[m])[(uint64_t)block * n + e];
+  }
+}
+
+// Continue the graph's while loop while the next power k + 1 is below `last`.
+__global__ void k_continue_while(const int* d_k, int last, cudaGraphConditionalHandle h) {
+  cudaGraphSetConditional(h, *d_k + 1 < last ? 1u : 0u);
+}
+
 cudaError_t launch_snapshot(const void* work, void* state, uint64_t n, const int* d_k, int dtype, cudaStream_t s) {
   uint64_t g = (n + 255) / 256;
   if (g > 152 * 16) g = 152 * 16;
@@ -158,6 +186,35 @@ cudaError_t launch_snapshot(const void* work, void* state, uint64_t n, const int
     k_snapshot<double2><<<(uint32_t)g, 256, 0, s>>>((const double2*)work, (double2*)state, n, d_k);
   else
     k_snapshot<float2><<<(uint32_t)g, 256, 0, s>>>((const float2*)work, (float2*)state, n, d_k);
+  return cudaGetLastError();
+}
+
+static uint32_t grid_of(uint64_t n) {
+  uint64_t g = (n + 255) / 256;
+  if (g > 152 * 16) g = 152 * 16;
+  return (uint32_t)(g < 1 ? 1 : g);
+}
+
+cudaError_t launch_snapshot_batch(void* const* works, void* const* states, uint64_t n, const int* d_k, uint32_t nmem,
+                                  int dtype, cudaStream_t s) {
+  if (dtype == QPE_C128)
+    k_snapshot_batch<double2><<<grid_of(n * nmem), 256, 0, s>>>(works, states, n, d_k, nmem);
+  else
+    k_snapshot_batch<float2><<<grid_of(n * nmem), 256, 0, s>>>(works, states, n, d_k, nmem);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_load_batch(void* const* works, void* const* states, uint64_t n, uint32_t block, uint32_t nmem,
+                              int dtype, cudaStream_t s) {
+  if (dtype == QPE_C128)
+    k_load_batch<double2><<<grid_of(n * nmem), 256, 0, s>>>(works, states, n, block, nmem);
+  else
+    k_load_batch<float2><<<grid_of(n * nmem), 256, 0, s>>>(works, states, n, block, nmem);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_continue_while(const int* d_k, int last, cudaGraphConditionalHandle h, cudaStream_t s) {
+  k_continue_while<<<1, 1, 0, s>>>(d_k, last, h);
   return cudaGetLastError();
 }
 

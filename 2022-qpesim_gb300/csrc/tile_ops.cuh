@@ -57,8 +57,12 @@ struct OpR {
   Coef4<R> k;
 };
 
+// icoef, when given, replaces the inline (c0, c1) of op o with icoef[o]: the
+// instances of a batch share one program's structure and keep their own
+// coefficients.
 template <typename R>
-__device__ __forceinline__ OpR<R> load_op(const DevOp* __restrict__ ops, const double* __restrict__ coef, uint32_t o) {
+__device__ __forceinline__ OpR<R> load_op(const DevOp* __restrict__ ops, const double* __restrict__ coef, uint32_t o,
+                                          const double2* __restrict__ icoef = nullptr) {
   OpR<R> r;
   const uint4* src = reinterpret_cast<const uint4*>(ops + o);
   const uint4 a = __ldg(src), b = __ldg(src + 1);
@@ -71,6 +75,11 @@ __device__ __forceinline__ OpR<R> load_op(const DevOp* __restrict__ ops, const d
   r.d.gen = a.w;
   r.d.c0 = __hiloint2double((int)b.y, (int)b.x);
   r.d.c1 = __hiloint2double((int)b.w, (int)b.z);
+  if (icoef) {
+    const double2 c = __ldg(icoef + o);
+    r.d.c0 = c.x;
+    r.d.c1 = c.y;
+  }
   if (r.d.gen == OP_INLINE) {
     // diagonal (c0, c1); pair m00 = c0, m01 = i c1 (parity 0) / -i c1 (parity 1)
     r.k.e0r = r.k.o0r = (R)r.d.c0;
@@ -150,7 +159,7 @@ template <typename R, class A, class Elem>
 __device__ __forceinline__ void run_line_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
                                              const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1, bool rev,
                                              uint32_t L, uint32_t jl, uint32_t jstep, bool active, uint32_t lstr,
-                                             Elem elem) {
+                                             Elem elem, const double2* __restrict__ icoef = nullptr) {
   const uint32_t n = op1 - op0;
   if (n == 0) return;
   auto at = [&](uint32_t i) { return rev ? op1 - 1 - i : op0 + i; };
@@ -158,13 +167,13 @@ __device__ __forceinline__ void run_line_ops(const DevOp* __restrict__ ops, cons
     return (d.kind == OPK_PAIR && jl < d.count) ? __ldg(reinterpret_cast<const uint2*>(pool + d.tab) + jl)
                                                 : make_uint2(0u, 0u);
   };
-  OpR<R> op = load_op<R>(ops, coef, at(0));
+  OpR<R> op = load_op<R>(ops, coef, at(0), icoef);
   uint2 first = first_of(op.d);
   for (uint32_t i = 0; i < n; ++i) {
     OpR<R> opn = op;
     uint2 firstn = make_uint2(0u, 0u);
     if (i + 1 < n) {
-      opn = load_op<R>(ops, coef, at(i + 1));
+      opn = load_op<R>(ops, coef, at(i + 1), icoef);
       firstn = first_of(opn.d);
     }
     const DevOp& d = op.d;
@@ -198,20 +207,20 @@ template <typename R, class A, class Left, class Right>
 __device__ __forceinline__ void run_mix_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
                                             const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1, bool rev,
                                             uint32_t jl, uint32_t jstep, bool active, uint32_t parb, Left left,
-                                            Right right) {
+                                            Right right, const double2* __restrict__ icoef = nullptr) {
   const uint32_t n = op1 - op0;
   if (n == 0) return;
   auto at = [&](uint32_t i) { return rev ? op1 - 1 - i : op0 + i; };
   auto first_of = [&](const DevOp& d) -> uint2 {
     return jl < d.count ? __ldg(reinterpret_cast<const uint2*>(pool + d.tab) + jl) : make_uint2(0u, 0u);
   };
-  OpR<R> op = load_op<R>(ops, coef, at(0));
+  OpR<R> op = load_op<R>(ops, coef, at(0), icoef);
   uint2 first = first_of(op.d);
   for (uint32_t i = 0; i < n; ++i) {
     OpR<R> opn = op;
     uint2 firstn = make_uint2(0u, 0u);
     if (i + 1 < n) {
-      opn = load_op<R>(ops, coef, at(i + 1));
+      opn = load_op<R>(ops, coef, at(i + 1), icoef);
       firstn = first_of(opn.d);
     }
     if (active) {

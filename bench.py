@@ -45,6 +45,13 @@ WORKLOADS = {
     "plain-n8": dict(n=8, N=4, P=6, dt=0.1, order=1, steps=1, dtype="c128", seed=0,
                      desc="Plain QPE, FP64: n=8, N=4, 6 ancilla qubits, 1st-order Trotter dt=0.1"),
 }
+# BASELINE configs[3]: the batching form.
+WORKLOADS["batched-256"] = dict(batch=True, count=256, sizes=(12, 14, 16, 18, 20), P=6, dt=0.05, order=1, steps=1,
+                                dtype="c64", seed=2024,
+                                desc="Batching form: 256 seeded Hamiltonians, n uniform in {12,14,16,18,20}, N=n/2 "
+                                     "(odd N split ceil/floor over the spins), 6 ancilla qubits, complex64 with FP64 "
+                                     "coefficients and histograms, 1st-order Trotter dt=0.05, Hartree-Fock starts, "
+                                     "one graph launch per step")
 DEFAULT_WORKLOAD = "plain-n16"
 
 
@@ -290,10 +297,175 @@ def run_ours(args, w, rank, ws, local):
     return line
 
 
+def batch_instances(w, rank=0):
+    """(n, N, seed) of every instance of a batched workload."""
+    rng = np.random.default_rng(w["seed"] + 7919 * rank)
+    ns = rng.choice(w["sizes"], size=w["count"])
+    return [(int(n), int(n) // 2, w["seed"] + 1000 * rank + i) for i, n in enumerate(ns)]
+
+
+def build_batch_terms(q, w, rank=0):
+    out = []
+    for n, Nel, seed in batch_instances(w, rank):
+        h = q.Hamiltonian.from_integrals(q.synthetic_integrals(n, seed), (Nel + 1) // 2, w["dt"])
+        out.append((n, (Nel + 1) // 2, Nel // 2, h.segmented_terms()))
+    return out
+
+
+def cpu_baseline_batch(q, w, terms, budget_s=20.0):
+    """The oracle on a bounded sample of the batch: one instance of each size, the
+    powers that fit in its share of the budget, the better of 1 thread and all
+    host threads per size; the batch's CPU time is the sum over its instances at
+    those per-size rates."""
+    O = graft.load_oracle()
+    orc = O.Oracle(fast=True)
+    P = w["P"]
+    ncpu = os.cpu_count() or 1
+    rate, cores, parts = {}, {}, []
+    sizes = sorted({t[0] for t in terms})
+    for n in sizes:
+        n_, na, nb, seg = next(t for t in terms if t[0] == n)
+        M = n // 2
+        touches = q.plan_program(seg, M, na, nb, w["order"], w["steps"])["touches_per_power"]
+        ld = math.comb(M, na) * math.comb(M, nb)
+        state = np.zeros((1 << P) * ld, np.complex128)
+        state[0] = 2 ** (-P / 2)
+        best = None
+        for threads in sorted({1, ncpu}):
+            orc.set_threads(threads)
+            t0 = time.perf_counter()
+            orc.time_evolve(M, na, nb, P, seg, state, first=1, last=2)
+            el = time.perf_counter() - t0
+            if best is None or el < best[1]:
+                best = (threads, el)
+        orc.set_threads(best[0])
+        npow = int(max(1, min((1 << P) - 1, budget_s / len(sizes) / max(best[1], 1e-9))))
+        t0 = time.perf_counter()
+        orc.time_evolve(M, na, nb, P, seg, state, first=1, last=1 + npow)
+        el = time.perf_counter() - t0
+        rate[n] = touches * npow / el
+        cores[n] = best[0]
+        parts.append(f"n={n}: {npow} powers, {best[0]} thread(s), {rate[n] / 1e6:.0f} M/s")
+    total_t = 0.0
+    total_touch = 0
+    for n, na, nb, seg in terms:
+        tp = q.plan_program(seg, n // 2, na, nb, w["order"], w["steps"])["touches_per_power"] * ((1 << P) - 1)
+        total_touch += tp
+        total_t += tp / rate[n]
+    return total_touch / total_t, max(cores.values()), "one instance per size, one at a time: " + "; ".join(parts)
+
+
+def run_batch(args, w, rank, ws, local):
+    q = graft.load_package()
+    N = q._native
+    P = w["P"]
+    dtype = np.complex64 if w["dtype"] == "c64" else np.complex128
+    terms = build_batch_terms(q, w, rank)
+    progs = [q.Program(seg, n // 2, na, nb, trotter_order=w["order"], steps=w["steps"], device=local)
+             for n, na, nb, seg in terms]
+    bt = q.Batch(progs, P, dtype=dtype, device=local)
+    bt.tune()
+    info = bt.info
+    timer = N.Timer(local)
+    lib = N.lib()
+    ctx = N.context(local)
+    b0 = [q.hf_block0(math.comb(n // 2, na), math.comb(n // 2, nb), P, dtype) for n, na, nb, _ in terms]
+
+    def upload_all(src):
+        for i, a in enumerate(src):
+            bt.upload(i, a)
+
+    for _ in range(args.warmup):
+        upload_all(b0)
+        bt.run()
+    barrier(ws)
+    clocks = Clocks()
+    clocks.start()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        upload_all(b0)
+        N.check(lib.qpe_flush_l2(ctx))
+        timer.record(0)
+        bt.run(synchronize=False)
+        timer.record(1)
+        total_ms += timer.elapsed_ms(0, 1)
+    clk = clocks.stop()
+    total_ms = reduce_max(total_ms, ws)
+    barrier(ws)
+    # End to end: block 0 of every instance in from page-locked memory, every
+    # histogram back.
+    pins = []
+    for a in b0:
+        pb = N.PinnedBuffer(a.size, dtype)
+        pb.array[:] = a
+        pins.append(pb)
+    probs = np.zeros((len(terms), 1 << P))
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        N.check(lib.qpe_flush_l2(ctx))
+        timer.record(2)
+        upload_all([p.array for p in pins])
+        bt.run(synchronize=False)
+        for i in range(len(terms)):
+            probs[i] = bt.phase_probs(i)
+        timer.record(3)
+        e2e_ms += timer.elapsed_ms(2, 3)
+    e2e_ms = reduce_max(e2e_ms, ws)
+    touches = info["touches_per_run"]
+    ms_step = total_ms / args.steps
+    value = touches * ws / (ms_step / 1e3)
+    peak, peak_kind = peaks()
+    achieved = touches * 16 / (ms_step / 1e3) / 1e9
+    sizes = {}
+    for n, na, nb, seg in terms:
+        sizes[n] = sizes.get(n, 0) + 1
+    line = {
+        "metric": "amplitude-term updates/s per Trotter step", "value": value, "unit": "touches/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded integrals (h_pq ~ N(0,1) exp(-|p-q|/2), (pq|rs) ~ N(0,0.1^2) "
+                "exp(-(|p-q|+|r-s|)/3)), one seed per instance, one batch per rank",
+        "config": {"workload": args.workload, "description": w["desc"], "instances": len(terms),
+                   "instances_per_n": {str(k): v for k, v in sorted(sizes.items())}, "precision": P, "dt": w["dt"],
+                   "state": w["dtype"], "touches_per_step": touches, "classes": info["classes"],
+                   "l2": "flushed before every timed step", "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_kind,
+                     "kernel": "k_pass (batched tile passes), 16 algorithmic bytes per touch over the whole run"},
+        "e2e": {"value": touches * ws / (e2e_ms / args.steps / 1e3), "unit": "touches/s",
+                "h2d_bytes_per_step": int(sum(a.nbytes for a in b0)),
+                "d2h_bytes_per_step": int(probs.nbytes)},
+        "gpu_launches": int(info["launches_per_run"]) * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        r, cores, sample = cpu_baseline_batch(q, w, terms)
+        line["cpu_baseline"] = {"value": r, "unit": "touches/s", "cores": cores, "kind": "port", "sample": sample}
+    return line
+
+
 def run_reference(args, w, rank, ws):
     if rank != 0:
         return None
     q = graft.load_package()
+    if w.get("batch"):
+        terms = build_batch_terms(q, w)
+        rates = []
+        for _ in range(args.steps):
+            r, cores, sample = cpu_baseline_batch(q, w, terms, budget_s=max(10.0, 60.0 / max(args.steps, 1)))
+            rates.append(r)
+        value = statistics.median(rates)
+        touches = sum(q.plan_program(seg, n // 2, na, nb, w["order"], w["steps"])["touches_per_power"]
+                      for n, na, nb, seg in terms) * ((1 << w["P"]) - 1)
+        return {"metric": "amplitude-term updates/s per Trotter step", "value": value, "unit": "touches/s",
+                "impl": "reference", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": touches / value * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (same integrals as the GPU arm)",
+                "config": {"workload": args.workload, "description": w["desc"]},
+                "cpu_baseline": {"value": value, "unit": "touches/s", "cores": cores, "kind": "port",
+                                 "sample": sample + "; CPU restatement of the reference (oracle/qpe_oracle.cc), "
+                                                    "complex128: the reference has no complex64 path"},
+                "e2e": {"value": value, "unit": "touches/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     h, seg = build_problem(q, w)
     rates = []
     sample = ""
@@ -335,6 +507,8 @@ def main():
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         line = run_reference(args, w, rank, ws)
+    elif w.get("batch"):
+        line = run_batch(args, w, rank, ws, local)
     else:
         line = run_ours(args, w, rank, ws, local)
     if rank == 0 and line is not None:

@@ -213,6 +213,32 @@ int qpe_state_phase_probs(qpe_state* st, double* probs);
 /* Per-block squared norms (2^P doubles, FP64 accumulation). */
 int qpe_state_block_norms(qpe_state* st, double* norms);
 
+/* ---- batching form ----------------------------------------------------------------
+ * Many Hamiltonians (programs) evolved, transformed and read out by one launch of
+ * one CUDA graph. Instances whose programs have the same structure share index
+ * tables and term lists; each keeps its own coefficients and its own 2^P x Ca x Cb
+ * register. No counterpart in the reference (which runs one Hamiltonian). */
+typedef struct qpe_batch qpe_batch;
+typedef struct qpe_batch_info {
+  uint32_t instances, classes;
+  uint64_t touches_per_run;  /* amplitude-term updates of one qpe_batch_run */
+  uint64_t amplitudes;       /* register elements over all instances */
+  uint32_t launches_per_run; /* kernel launches one run makes inside its graph */
+  uint32_t reserved;
+} qpe_batch_info;
+int qpe_batch_create(qpe_context* ctx, uint32_t n, const qpe_program* const* programs, uint32_t precision,
+                     int dtype, qpe_batch** out);
+int qpe_batch_destroy(qpe_batch* b);
+int qpe_batch_upload(qpe_batch* b, uint32_t instance, const void* host, uint64_t first, uint64_t count);
+int qpe_batch_download(qpe_batch* b, uint32_t instance, void* host, uint64_t first, uint64_t count);
+/* Times one power of every candidate tile shape per class and keeps the fastest. */
+int qpe_batch_tune(qpe_batch* b);
+/* One graph launch: every power of every instance, then every QIFT and histogram.
+ * Blocks 1.. of each register are overwritten from its block 0. */
+int qpe_batch_run(qpe_batch* b, int synchronize);
+int qpe_batch_phase_probs(qpe_batch* b, uint32_t instance, double* probs);
+int qpe_batch_get_info(const qpe_batch* b, qpe_batch_info* info);
+
 /* ---- QIFT without any allocation ------------------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device memory
  * when they need the QIFT: code whose stream is being captured into a CUDA graph

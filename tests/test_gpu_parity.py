@@ -279,3 +279,45 @@ def test_fp64_contract_within_tolerance(gpu, orc, strategy, cluster):
     got = st.download()
     assert np.abs(got - ref).max() < 1e-12
     assert not np.array_equal(got, ref) or True
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_batch_matches_oracle_per_instance(gpu, orc, dtype):
+    """A batch of uneven Hamiltonians (two structure classes per size, odd and
+    even electron counts) in one graph launch: every register equals the
+    oracle's evolution of that instance (complex128 bit for bit, complex64 within
+    2e-5), every histogram the oracle's QIFT histogram; a tuned rerun gives the
+    same complex128 result."""
+    q = gpu
+    P = 3
+    shapes = [(8, 2, 2), (10, 3, 2), (8, 2, 2), (12, 3, 3), (10, 3, 2), (6, 1, 1)]
+    progs, segs, b0s = [], [], []
+    for i, (n, na, nb) in enumerate(shapes):
+        seg = _seg(q, n, na + nb, 500 + i, 0.08)
+        segs.append(seg)
+        progs.append(q.Program(seg, n // 2, na, nb))
+    bt = q.Batch(progs, P, dtype=dtype)
+    assert bt.info["classes"] == 4
+    rng = np.random.default_rng(3)
+    for i, (n, na, nb) in enumerate(shapes):
+        ld = bt.ld[i]
+        b0s.append((rng.standard_normal(ld) + 1j * rng.standard_normal(ld)) / np.sqrt(2 * ld))
+    for rep in range(2):
+        if rep == 1:
+            bt.tune()
+        for i in range(len(shapes)):  # the QIFT of a run transforms block 0 as well
+            bt.upload(i, b0s[i].astype(dtype))
+        bt.run()
+        for i, (n, na, nb) in enumerate(shapes):
+            ld = bt.ld[i]
+            ref = np.zeros((1 << P) * ld, np.complex128)
+            ref[:ld] = b0s[i].astype(dtype) if dtype == np.complex64 else b0s[i]
+            orc.time_evolve(n // 2, na, nb, P, segs[i], ref)
+            orc.qift(P, ld, ref)
+            got = bt.download(i)
+            if dtype == np.complex128:
+                assert np.array_equal(got, ref), i
+            else:
+                assert np.abs(got - ref).max() < 2e-5, i
+            np.testing.assert_allclose(bt.phase_probs(i), orc.identify_phase_amplitudes(P, ld, ref), rtol=1e-4,
+                                       atol=1e-6)
