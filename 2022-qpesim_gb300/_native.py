@@ -97,6 +97,8 @@ PROTOTYPES = {
     "qpe_ham_destroy": (C.c_int, [_vp]),
     "qpe_ham_add_one_body": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double]),
     "qpe_ham_add_two_body": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]),
+    "qpe_ham_ingest_broombridge": (C.c_int, [_vp, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), _PD,
+                                             C.c_size_t]),
     "qpe_ham_set_num_orbitals": (C.c_int, [_vp, C.c_uint32]),
     "qpe_ham_set_num_occupied": (C.c_int, [_vp, C.c_uint32]),
     "qpe_ham_set_identity": (C.c_int, [_vp, C.c_double]),

@@ -6,7 +6,9 @@
 // device program are the ones the reference would compute.
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
+#include <regex>
 #include <map>
 #include <new>
 #include <set>
@@ -16,8 +18,17 @@
 
 #include "../../include/qpe_gb300_hamiltonian.h"
 #include "qpe_common.h"
+#include "yaml_subset.h"
 
 namespace qpe {
+
+static uint64_t binom_exact(int n, int k) {
+  if (k < 0 || n < 0 || k > n) return 0;
+  if (k * 2 > n) k = n - k;
+  uint64_t r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (uint64_t)(n - k + i) / (uint64_t)i;
+  return r;
+}
 
 // SpinOrbital (cpp/types.hpp:33-98): ordered by spin (Up < Down), then orbital.
 struct SpinOrb {
@@ -245,6 +256,15 @@ static void put2(const std::complex<double>* m, double* dst) {
   dst[3] = m[1].imag();
 }
 
+// rank of a bit string (cpp/offset_computer.hpp:16-27), for the initial state.
+static int64_t colex_rank(uint64_t bv) {
+  int64_t r = 0;
+  int order = 1;
+  for (int pos = 0; bv; ++pos, bv >>= 1)
+    if (bv & 1) r += (int64_t)binom_exact(pos, order++);
+  return r;
+}
+
 }  // namespace qpe
 
 using qpe::Hamiltonian;
@@ -397,6 +417,112 @@ int qpe_ham_segment_terms(const qpe_hamiltonian* h, int kind, qpe_term* out, dou
           H.pqrs_term(p, q, r, s, 1, m);
           qpe::put2(m, t.odd);
         }
+      }
+    }
+  });
+}
+
+// IngestBroombridge (cpp/hamiltonian.cc:8-144) over the project's YAML reader:
+// identity, one-body rows [p, q, v] (swapped so p >= q), two-body rows
+// [i, l, j, k, v] -> AddTwoBodyTerm(i, j, k, l), the orbital count as the largest
+// index seen, and the first initial-state suggestion with its Jordan-Wigner signs
+// (operators applied right to left; each one flips the sign once per occupied
+// orbital below it), addressed at C(M, e) * rank(alpha) + rank(beta).
+int qpe_ham_ingest_broombridge(qpe_hamiltonian* hh, const char* path, uint32_t* num_orbitals, uint32_t* num_occupied,
+                               double* block0, size_t cap) {
+  return qpe::guard([&] {
+    if (!hh || !path) throw qpe::Error(QPE_ERR_INVALID, "null argument");
+    Hamiltonian& H = hh->h;
+    std::shared_ptr<const qpe_yaml::Value> doc;
+    try {
+      doc = qpe_yaml::load_file(path);
+    } catch (const std::exception& e) {
+      throw qpe::Error(QPE_ERR_INVALID, e.what());
+    }
+    auto need = [](const qpe_yaml::Value* v, const char* what) {
+      if (!v) throw qpe::Error(QPE_ERR_INVALID, std::string("Broombridge file lacks ") + what);
+      return v;
+    };
+    auto num = [&](const qpe_yaml::Value* v, const char* what) {
+      need(v, what);
+      if (v->kind != qpe_yaml::Value::Scalar) throw qpe::Error(QPE_ERR_INVALID, std::string(what) + " is not a number");
+      return std::strtod(v->scalar.c_str(), nullptr);
+    };
+    const qpe_yaml::Value* sets = need(doc->get("integral_sets"), "integral_sets");
+    const qpe_yaml::Value* ints = need(sets->at(0), "integral_sets[0]");
+    H.identity = num(need(ints->get("coulomb_repulsion"), "coulomb_repulsion")->get("value"), "coulomb_repulsion") +
+                 num(need(ints->get("energy_offset"), "energy_offset")->get("value"), "energy_offset");
+    const qpe_yaml::Value* ham = need(ints->get("hamiltonian"), "hamiltonian");
+    unsigned maxorb = H.num_orbitals;
+    const qpe_yaml::Value* ob = need(need(ham->get("one_electron_integrals"), "one_electron_integrals")->get("values"),
+                                     "one_electron_integrals.values");
+    for (const auto& row : ob->seq) {
+      unsigned p = (unsigned)num(row->at(0), "index"), q = (unsigned)num(row->at(1), "index");
+      const double v = num(row->at(2), "value");
+      if (q > p) std::swap(p, q);
+      H.add_one((int)p, (int)q, v);
+      maxorb = std::max(maxorb, std::max(p, q));
+    }
+    const qpe_yaml::Value* tb = need(need(ham->get("two_electron_integrals"), "two_electron_integrals")->get("values"),
+                                     "two_electron_integrals.values");
+    for (const auto& row : tb->seq) {
+      const unsigned i = (unsigned)num(row->at(0), "index"), l = (unsigned)num(row->at(1), "index");
+      const unsigned j = (unsigned)num(row->at(2), "index"), k = (unsigned)num(row->at(3), "index");
+      H.add_two((int)i, (int)j, (int)k, (int)l, num(row->at(4), "value"));
+      maxorb = std::max(maxorb, std::max(std::max(i, j), std::max(k, l)));
+    }
+    if (maxorb == 0 || maxorb > 31) throw qpe::Error(QPE_ERR_UNSUPPORTED, "orbital count must be in 1..31");
+    H.num_orbitals = maxorb;
+    // Initial state (cpp/hamiltonian.cc:54-139).
+    std::vector<std::pair<uint64_t, double>> amps;
+    const qpe_yaml::Value* sugg = ints->get("initial_state_suggestions");
+    const qpe_yaml::Value* sup = nullptr;
+    if (sugg && sugg->at(0) && sugg->at(0)->get("state")) sup = sugg->at(0)->get("state")->get("superposition");
+    static const std::regex pat(R"(\((\d+)([ab])\)(\+*))");
+    if (sup) {
+      for (const auto& basis : sup->seq) {
+        if (basis->kind != qpe_yaml::Value::Seq || basis->seq.size() < 2) continue;
+        double coeff = num(basis->at(0), "coefficient");
+        unsigned electrons = 0;
+        uint64_t bv = 0;
+        for (size_t t = basis->seq.size() - 1; t-- > 1;) {  // operators, right to left
+          std::smatch m;
+          const std::string& txt = basis->seq[t]->scalar;
+          if (!std::regex_match(txt, m, pat)) throw qpe::Error(QPE_ERR_INVALID, "bad operator " + txt);
+          const unsigned orb = (unsigned)std::stoi(m[1]) - 1;
+          const bool up = m[2] == "a";
+          const bool raise = m[3] == "+";
+          const unsigned idx = up ? orb : orb + maxorb;
+          if (idx >= 64) throw qpe::Error(QPE_ERR_INVALID, "orbital index out of range");
+          if (raise) {
+            if ((bv >> idx) & 1) throw qpe::Error(QPE_ERR_INVALID, "creation on an occupied orbital");
+            bv += 1ull << idx;
+            ++electrons;
+          } else {
+            if (!((bv >> idx) & 1)) throw qpe::Error(QPE_ERR_INVALID, "annihilation on an empty orbital");
+            bv -= 1ull << idx;
+            --electrons;
+          }
+          for (unsigned pos = 0; pos < idx; ++pos)
+            if ((bv >> pos) & 1) coeff *= -1.0;
+        }
+        H.num_occupied = electrons / 2;
+        const uint64_t beta = bv >> maxorb, alpha = bv & ((1ull << maxorb) - 1);
+        const uint64_t addr = qpe::binom_exact((int)maxorb, (int)H.num_occupied) * (uint64_t)qpe::colex_rank(alpha) +
+                              (uint64_t)qpe::colex_rank(beta);
+        amps.emplace_back(addr, coeff);
+      }
+    }
+    if (num_orbitals) *num_orbitals = H.num_orbitals;
+    if (num_occupied) *num_occupied = H.num_occupied;
+    if (block0) {
+      const uint64_t C = qpe::binom_exact((int)H.num_orbitals, (int)H.num_occupied);
+      if (cap < C * C) throw qpe::Error(QPE_ERR_INVALID, "block0 capacity below C(M, e)^2");
+      std::memset(block0, 0, 2 * C * C * sizeof(double));
+      for (const auto& a : amps) {
+        if (a.first >= C * C) throw qpe::Error(QPE_ERR_INVALID, "initial state outside the register");
+        block0[2 * a.first] = a.second;
+        block0[2 * a.first + 1] = 0.0;
       }
     }
   });

@@ -50,10 +50,21 @@ class Hamiltonian:
         N.check(self._lib.qpe_ham_index_terms(self._h))
 
     def IngestBroombridge(self, filepath, precision: int = 5):
-        """Reads a Broombridge file (cpp/hamiltonian.cc:8-144); returns the
-        StateVector with the first initial-state suggestion in block 0."""
-        from .broombridge import ingest_broombridge
-        return ingest_broombridge(self, filepath, precision)
+        """Reads a Broombridge file (cpp/hamiltonian.cc:8-144) with the native
+        reader; returns the StateVector with the first initial-state suggestion
+        (Jordan-Wigner signs applied) in block 0."""
+        from .state_vector import StateVector
+        path = str(filepath).encode()
+        m, e = C.c_uint32(), C.c_uint32()
+        probe = Hamiltonian()
+        N.check(self._lib.qpe_ham_ingest_broombridge(probe._h, path, C.byref(m), C.byref(e), None, 0))
+        sv = StateVector(precision, m.value, e.value)
+        blk = np.zeros(sv.ld, np.complex128)
+        N.check(self._lib.qpe_ham_ingest_broombridge(self._h, path, None, None,
+                                                     blk.view(np.float64).ctypes.data_as(C.POINTER(C.c_double)),
+                                                     sv.ld))
+        sv[:sv.ld] = blk
+        return sv
 
     # ---- fields the reference sets while ingesting (cpp/hamiltonian.hpp:144-150) ----
     def SetNumOrbitals(self, m: int) -> None:

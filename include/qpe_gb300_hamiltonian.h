@@ -35,6 +35,15 @@ int qpe_ham_add_one_body(qpe_hamiltonian* h, int p, int q, double coeff);
  * and 1/4 factors. A Broombridge row [i, l, j, k, v] is AddTwoBodyTerm(i, j, k, l). */
 int qpe_ham_add_two_body(qpe_hamiltonian* h, int p, int q, int r, int s, double coeff);
 
+/* IngestBroombridge(path, precision) (cpp/hamiltonian.cc:8-144): adds the file's
+ * one- and two-body terms, sets the identity term, the orbital count (the largest
+ * index in the file) and the electrons per spin (from the first initial-state
+ * suggestion), and, if block0 is given (capacity in complex elements), writes
+ * that suggestion with its Jordan-Wigner signs as block 0 of the register
+ * (C(M, e)^2 interleaved complex doubles, unscaled). Call IndexTerms afterwards. */
+int qpe_ham_ingest_broombridge(qpe_hamiltonian* h, const char* path, uint32_t* num_orbitals,
+                               uint32_t* num_occupied, double* block0, size_t cap);
+
 /* Fields IngestBroombridge sets from the file (cpp/hamiltonian.cc:13-36, :113-115). */
 int qpe_ham_set_num_orbitals(qpe_hamiltonian* h, uint32_t num_orbitals);
 /* SetNumOccupied (cpp/hamiltonian.hpp:69): electrons per spin. */
