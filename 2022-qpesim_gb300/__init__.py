@@ -17,13 +17,14 @@ from .readout import (argmax_phase, margin_of_error, phase_to_energy, reference_
                       subbin_phase, success_probability)
 from .state_vector import StateVector
 from .synthetic import Integrals, hf_block0, synthetic_integrals
-from .time_evolution import DeviceState, Program, plan_program, time_evolve_over_terms
+from .time_evolution import DeviceState, Program, plan_program, time_evolve_iqpe, time_evolve_over_terms
 
 QpeError = _native.QpeError
 TERM_DTYPE = _native.TERM_DTYPE
 LIB_PATH = _native.LIB_PATH
 
-__all__ = ["Batch", "Hamiltonian", "SpinIndex", "OffsetComputer", "StateVector", "time_evolve_over_terms", "Program",
+__all__ = ["Batch", "Hamiltonian", "SpinIndex", "OffsetComputer", "StateVector", "time_evolve_over_terms",
+           "time_evolve_iqpe", "Program",
            "DeviceState", "plan_program", "Integrals", "synthetic_integrals", "hf_block0", "QpeError", "TERM_DTYPE",
            "reference_phase", "reference_energy", "margin_of_error", "phase_to_energy", "argmax_phase",
            "subbin_phase", "success_probability"]

@@ -43,7 +43,11 @@ class ProgramInfo(C.Structure):
 
 class EvolveOpts(C.Structure):
     _fields_ = [("strategy", C.c_uint32), ("first_power", C.c_uint32), ("last_power", C.c_uint32),
-                ("cluster_size", C.c_uint32), ("flags", C.c_uint32)]
+                ("cluster_size", C.c_uint32), ("flags", C.c_uint32), ("repeats", C.c_uint32)]
+
+
+QPE_EVOLVE_FP64_CONTRACT, QPE_EVOLVE_IN_PLACE = 1, 2
+QPE_PROGRAM_APPLY_UNITARY_ORDER = 0x100
 
 
 TERM_DTYPE = np.dtype([("p", "<u4"), ("q", "<u4"), ("r", "<u4"), ("s", "<u4"),
@@ -75,6 +79,8 @@ PROTOTYPES = {
                                  C.POINTER(C.c_uint32), C.POINTER(C.c_uint8), C.c_size_t, C.POINTER(C.c_size_t)]),
     "qpe_time_evolve_over_terms": (C.c_int, [_vp, C.c_uint32, C.c_uint32, C.c_uint32] + [_P_TERM, C.c_size_t] * 5
                                    + [_PD]),
+    "qpe_time_evolve_iqpe": (C.c_int, [_vp, C.c_uint32, C.c_uint32, C.c_uint32] + [_P_TERM, C.c_size_t] * 5
+                             + [C.c_uint32, _PD]),
     "qpe_qift": (C.c_int, [_vp, C.c_uint32, C.c_uint64, _PD]),
     "qpe_identify_phase_amplitudes": (C.c_int, [_vp, C.c_uint32, C.c_uint64, _PD, _PD]),
     "qpe_program_create": (C.c_int, [_vp, C.c_uint32, C.c_uint32, C.c_uint32] + [_P_TERM, C.c_size_t] * 5

@@ -240,9 +240,9 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
 }
 
 static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint32_t first, uint32_t last,
-                         bool exact) {
+                         bool exact, bool in_place = false) {
   ResidentLaunch rl;
-  ResidentInstance ri;
+  ResidentInstance ri{};
   if (!plan_resident(pr, st, K, rl, ri)) throw Error(QPE_ERR_UNSUPPORTED, "block does not fit the cluster's shared memory");
   ri.state = st->data.p;
   ri.pool = pr->pool.as<uint32_t>();
@@ -256,6 +256,7 @@ static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint3
   ri.last = last;
   ri.steps = pr->hp.steps;
   ri.order = pr->hp.order;
+  ri.in_place = in_place ? 1u : 0u;
   if (!st->res_inst.p) st->res_inst.alloc(sizeof(ResidentInstance));
   QPE_CK(cudaMemcpyAsync(st->res_inst.p, &ri, sizeof(ri), cudaMemcpyHostToDevice, st->ctx->stream));
   rl.insts = st->res_inst.as<ResidentInstance>();
@@ -266,7 +267,8 @@ static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint3
   QPE_CK(launch_resident(rl, st->dtype, exact, st->ctx->stream));
 }
 
-static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last, bool exact);
+static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last, bool exact,
+                         bool in_place = false);
 
 // Strategy for (program, state): explicit, or timed on one power per candidate.
 static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts, bool exact,
@@ -274,7 +276,7 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
   strategy = opts ? opts->strategy : QPE_STRATEGY_AUTO;
   K = opts ? opts->cluster_size : 0;
   ResidentLaunch rl;
-  ResidentInstance ri;
+  ResidentInstance ri{};
   if (strategy == QPE_STRATEGY_RESIDENT) {
     K = 1;
     return;
@@ -293,8 +295,17 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     K = st->tuned_cluster;
     return;
   }
-  // Autotune: time one power of every feasible candidate (block 1 is rewritten
-  // by the real run afterwards), the tiled strategy included.
+  // Autotune: time one power of every feasible candidate, the tiled strategy
+  // included. The trial powers write block 1, which is saved first and put back
+  // afterwards, so that tuning leaves the register as it was.
+  DevBuf saved;
+  saved.alloc(st->ld * st->esz);
+  char* block1 = st->data.as<char>() + st->ld * st->esz;
+  QPE_CK(cudaMemcpyAsync(saved.p, block1, st->ld * st->esz, cudaMemcpyDeviceToDevice, st->ctx->stream));
+  struct Restore {
+    void* dst; const void* src; size_t n; cudaStream_t s;
+    ~Restore() { cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, s); cudaStreamSynchronize(s); }
+  } restore{block1, saved.p, st->ld * st->esz, st->ctx->stream};
   std::vector<std::pair<uint32_t, uint32_t>> cands;
   for (uint32_t c = 1; c <= 16; c *= 2)
     if (plan_resident(pr, st, c, rl, ri)) cands.push_back({c == 1 ? QPE_STRATEGY_RESIDENT : QPE_STRATEGY_CLUSTER, c});
@@ -346,34 +357,47 @@ static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* 
   const HostProgram& hp = pr->hp;
   if (hp.M != st->M || hp.na != st->na || hp.nb != st->nb)
     throw Error(QPE_ERR_INVALID, "program and state shapes differ");
+  const bool in_place = opts && (opts->flags & QPE_EVOLVE_IN_PLACE);
   uint32_t first = 1, last = (uint32_t)st->N;
-  if (opts && (opts->first_power || opts->last_power)) {
+  if (in_place) {
+    // Block first_power, evolved `repeats` times: the kernels see the range
+    // [first, first + repeats) and write every power back to block first.
     first = opts->first_power;
-    last = opts->last_power;
+    const uint32_t reps = opts->repeats ? opts->repeats : 1u;
+    if (first >= st->N) throw Error(QPE_ERR_INVALID, "in-place block outside 0 .. 2^P - 1");
+    if (reps > (1u << 30)) throw Error(QPE_ERR_INVALID, "repeats above 2^30");
+    last = first + reps;
+  } else {
+    if (opts && (opts->first_power || opts->last_power)) {
+      first = opts->first_power;
+      last = opts->last_power;
+    }
+    if (first < 1 || last > st->N || first > last) throw Error(QPE_ERR_INVALID, "power range outside 1 .. 2^P");
   }
-  if (first < 1 || last > st->N || first > last) throw Error(QPE_ERR_INVALID, "power range outside 1 .. 2^P");
   st->probs_valid = false;
   if (first == last) return;
   const bool exact = st->dtype == QPE_C128 && !(opts && (opts->flags & QPE_EVOLVE_FP64_CONTRACT));
   uint32_t strategy = 0, K = 0;
   choose_strategy(st, pr, opts, exact, strategy, K);
   if (strategy == QPE_STRATEGY_TILED) {
-    evolve_tiled(st, pr, first, last, exact);
+    evolve_tiled(st, pr, first, last, exact, in_place);
   } else {
-    run_resident(st, pr, K, first, last, exact);
+    run_resident(st, pr, K, first, last, exact, in_place);
     QPE_CK(cudaStreamSynchronize(st->ctx->stream));
   }
 }
 
 // Global-memory working block, one kernel launch per pass, one captured graph
 // per controlled power replayed for every power.
-static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last, bool exact) {
+static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last, bool exact,
+                         bool in_place) {
   const HostProgram& hp = pr->hp;
   cudaStream_t s = st->ctx->stream;
   if (!st->work.p) st->work.alloc(st->ld * st->esz);
-  // Working block <- block first - 1.
-  QPE_CK(cudaMemcpyAsync(st->work.p, st->data.as<char>() + (size_t)(first - 1) * st->ld * st->esz,
-                         st->ld * st->esz, cudaMemcpyDeviceToDevice, s));
+  // Working block <- block first - 1 (block first when evolving in place).
+  const size_t src = in_place ? first : first - 1;
+  QPE_CK(cudaMemcpyAsync(st->work.p, st->data.as<char>() + src * st->ld * st->esz, st->ld * st->esz,
+                         cudaMemcpyDeviceToDevice, s));
   k_set_int<<<1, 1, 0, s>>>(st->dk.as<int>(), (int)first);
   QPE_CK(cudaGetLastError());
   if (st->graph_prog != pr->id || st->graph_exact != (uint32_t)exact || !st->graph) {
@@ -416,7 +440,14 @@ static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, u
     st->graph_prog = pr->id;
     st->graph_exact = exact;
   }
-  for (uint32_t k = first; k < last; ++k) QPE_CK(cudaGraphLaunch(st->graph, s));
+  for (uint32_t k = first; k < last; ++k) {
+    // In place, every power's snapshot targets block first again.
+    if (in_place && k > first) {
+      k_set_int<<<1, 1, 0, s>>>(st->dk.as<int>(), (int)first);
+      QPE_CK(cudaGetLastError());
+    }
+    QPE_CK(cudaGraphLaunch(st->graph, s));
+  }
   QPE_CK(cudaStreamSynchronize(s));
 }
 
@@ -874,6 +905,41 @@ int qpe_time_evolve_over_terms(qpe_context* ctx, uint32_t M, uint32_t e, uint32_
     rc = qpe_state_upload(st, state, 0, ld);
     if (!rc) rc = qpe_evolve(st, pr, nullptr);
     if (!rc) rc = qpe_state_download(st, state, 0, total);
+    std::string msg = g_last_error;
+    qpe_state_destroy(st);
+    qpe_program_destroy(pr);
+    if (rc) throw Error(rc, msg);
+  });
+}
+
+int qpe_time_evolve_iqpe(qpe_context* ctx, uint32_t M, uint32_t e, uint32_t P, const qpe_term* pp, size_t n_pp,
+                         const qpe_term* pq, size_t n_pq, const qpe_term* pqqp, size_t n_pqqp, const qpe_term* pqqr,
+                         size_t n_pqqr, const qpe_term* pqrs, size_t n_pqrs, uint32_t applications, double* state) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (!state) throw Error(QPE_ERR_INVALID, "null state");
+    if (P == 0) throw Error(QPE_ERR_INVALID, "time_evolve_iqpe needs precision >= 1 (it evolves block 1)");
+    if (applications == 0) return;
+    qpe_program* pr = nullptr;
+    qpe_state* st = nullptr;
+    int rc = qpe_program_create(ctx, M, e, e, pp, n_pp, pq, n_pq, pqqp, n_pqqp, pqqr, n_pqqr, pqrs, n_pqrs,
+                                1u | QPE_PROGRAM_APPLY_UNITARY_ORDER, 1, &pr);
+    if (rc) throw Error(rc, g_last_error);
+    // Only block 1 takes part: a two-block device register holds it.
+    rc = qpe_state_create(ctx, M, e, e, 1, QPE_C128, &st);
+    if (rc) {
+      qpe_program_destroy(pr);
+      throw Error(rc, g_last_error);
+    }
+    const uint64_t ld = st->ld;
+    double* block1 = state + 2 * ld;
+    rc = qpe_state_upload(st, block1, ld, ld);
+    qpe_evolve_opts o{};
+    o.flags = QPE_EVOLVE_IN_PLACE;
+    o.first_power = 1;
+    o.repeats = applications;
+    if (!rc) rc = qpe_evolve(st, pr, &o);
+    if (!rc) rc = qpe_state_download(st, block1, ld, ld);
     std::string msg = g_last_error;
     qpe_state_destroy(st);
     qpe_program_destroy(pr);

@@ -162,11 +162,14 @@ void build_graph(qpe_batch* b) {
   size_t smem = 48 * 1024;
   for (BatchClass& c : b->classes) smem = std::max(smem, plans_smem(b, c));
   QPE_CK(configure_pass_kernels(b->dtype, smem));
+  // One shared-memory limit for every instance's QIFT: the largest tile's.
   uint32_t T = 1, grid = 1;
+  size_t qsmem = 0;
   for (uint32_t i = 0; i < b->n; ++i) {
     qift_geometry(b->P, b->ld[i], b->dtype, b->ctx->num_sms, b->ctx->smem_optin, T, grid);
-    QPE_CK(configure_qift_kernels(b->dtype, qift_smem_bytes(b->P, T, b->dtype)));
+    qsmem = std::max(qsmem, qift_smem_bytes(b->P, T, b->dtype));
   }
+  QPE_CK(configure_qift_kernels(b->dtype, qsmem));
   const int last = (int)b->N;
   b->launches_per_run = 0;
   QPE_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));

@@ -14,6 +14,9 @@
 // a real m00 and an imaginary m01 (every pq / pqqr / pqrs term the Hamiltonian
 // getters produce) skip the products with exact zeros, which changes no bit.
 #include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
 #include <stdint.h>
 
 #include "kernels.h"
@@ -131,13 +134,26 @@ static cudaError_t configure_typed(size_t smem) {
   return cudaFuncSetAttribute(k_pass<R, A, PASS_MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
+// The shared-memory limit is a property of the kernel, not of one launch or one
+// captured graph, so it only ever grows: a later, smaller request must not break
+// the launches (and graphs) planned for a larger one.
 cudaError_t configure_pass_kernels(int dtype, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, size_t> granted;  // (device, dtype) -> bytes
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& g = granted[{dev, dtype}];
+  if (smem <= g) return cudaSuccess;
+  cudaError_t e;
   if (dtype == QPE_C128) {
-    cudaError_t e = configure_typed<double, ExactD>(smem);
-    if (e) return e;
-    return configure_typed<double, Fast<double>>(smem);
+    e = configure_typed<double, ExactD>(smem);
+    if (e == cudaSuccess) e = configure_typed<double, Fast<double>>(smem);
+  } else {
+    e = configure_typed<float, Fast<float>>(smem);
   }
-  return configure_typed<float, Fast<float>>(smem);
+  if (e == cudaSuccess) g = smem;
+  return e;
 }
 
 // Snapshot of the working block into block *d_k of the state

@@ -77,6 +77,8 @@ struct ResidentInstance {
   uint32_t rows_per_cta;    // rows owned by each CTA of the cluster
   uint32_t Wc, Wr, Wm;
   uint32_t steps, order;    // Trotter steps per power; 2 = forward + backward sweep
+  uint32_t in_place;        // 1: block `first` is loaded, evolved last - first times
+                            //    and written back to itself (iterative QPE)
 };
 struct ResidentLaunch {
   const ResidentInstance* insts;  // device array, ninst entries

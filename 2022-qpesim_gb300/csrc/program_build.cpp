@@ -268,25 +268,9 @@ struct Builder {
 
 }  // namespace
 
-void build_program(HostProgram& P, unsigned M, unsigned na, unsigned nb, const TermArrays& T,
-                   unsigned order, unsigned steps) {
-  if (M == 0 || M > 31) throw Error(QPE_ERR_INVALID, "num_orbitals must be in 1..31");
-  if (na == 0 || nb == 0 || na > M || nb > M) throw Error(QPE_ERR_INVALID, "electrons per spin must be in 1..M");
-  if (order != 1 && order != 2) throw Error(QPE_ERR_INVALID, "trotter_order must be 1 or 2");
-  if (steps == 0 || steps > 4096) throw Error(QPE_ERR_INVALID, "steps_per_power must be in 1..4096");
-  P = HostProgram{};
-  P.M = M;
-  P.na = na;
-  P.nb = nb;
-  P.Ca = binom((int)M, (int)na);
-  P.Cb = binom((int)M, (int)nb);
-  if (P.Ca > 0x7fffffffull || P.Cb > 0x7fffffffull) throw Error(QPE_ERR_UNSUPPORTED, "string space too large");
-  P.order = order;
-  P.steps = steps;
-  Builder B(P);
-
-  // The application order of applyUnitary_reordered (:374-562).
-  std::vector<AbsOp> sweep;
+// The application order of applyUnitary_reordered (:374-562).
+static void reordered_sweep(Builder& B, const TermArrays& T, std::vector<AbsOp>& sweep) {
+  const unsigned M = B.P.M;
   AbsOp op;
   for (size_t i = 0; i < T.n[QPE_TERM_PP]; ++i)
     if (B.lower(QPE_TERM_PP, T.t[QPE_TERM_PP][i], op)) sweep.push_back(op);
@@ -309,6 +293,38 @@ void build_program(HostProgram& P, unsigned M, unsigned na, unsigned nb, const T
   }
   for (size_t i = 0; i < T.n[QPE_TERM_PQRS]; ++i)
     if (B.lower(QPE_TERM_PQRS, T.t[QPE_TERM_PQRS][i], op)) sweep.push_back(op);
+}
+
+void build_program(HostProgram& P, unsigned M, unsigned na, unsigned nb, const TermArrays& T,
+                   unsigned order, unsigned steps) {
+  const bool au_order = (order & QPE_PROGRAM_APPLY_UNITARY_ORDER) != 0;
+  order &= ~QPE_PROGRAM_APPLY_UNITARY_ORDER;
+  if (M == 0 || M > 31) throw Error(QPE_ERR_INVALID, "num_orbitals must be in 1..31");
+  if (na == 0 || nb == 0 || na > M || nb > M) throw Error(QPE_ERR_INVALID, "electrons per spin must be in 1..M");
+  if (order != 1 && order != 2) throw Error(QPE_ERR_INVALID, "trotter_order must be 1 or 2");
+  if (steps == 0 || steps > 4096) throw Error(QPE_ERR_INVALID, "steps_per_power must be in 1..4096");
+  P = HostProgram{};
+  P.M = M;
+  P.na = na;
+  P.nb = nb;
+  P.Ca = binom((int)M, (int)na);
+  P.Cb = binom((int)M, (int)nb);
+  if (P.Ca > 0x7fffffffull || P.Cb > 0x7fffffffull) throw Error(QPE_ERR_UNSUPPORTED, "string space too large");
+  P.order = order;
+  P.steps = steps;
+  P.apply_unitary_order = au_order;
+  Builder B(P);
+
+  std::vector<AbsOp> sweep;
+  AbsOp op;
+  if (au_order) {
+    // The order of applyUnitary (:174-372): each segment whole, in map order.
+    for (int kind : {QPE_TERM_PP, QPE_TERM_PQ, QPE_TERM_PQQP, QPE_TERM_PQQR, QPE_TERM_PQRS})
+      for (size_t i = 0; i < T.n[kind]; ++i)
+        if (B.lower(kind, T.t[kind][i], op)) sweep.push_back(op);
+  } else {
+    reordered_sweep(B, T, sweep);
+  }
 
   P.ops_per_sweep = (uint32_t)sweep.size();
   for (const AbsOp& a : sweep) P.touches_per_sweep += a.touches;

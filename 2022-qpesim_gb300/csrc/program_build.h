@@ -22,6 +22,7 @@ struct HostProgram {
   unsigned M = 0, na = 0, nb = 0;
   uint64_t Ca = 0, Cb = 0;
   unsigned order = 1, steps = 1;
+  bool apply_unitary_order = false;  // applyUnitary's term order (iterative QPE)
   std::vector<AxisTable> tables;
   uint64_t pool_words = 0;
   std::vector<DevOp> ops;      // one forward Trotter sweep

@@ -18,6 +18,9 @@
 // std::complex<double> arithmetic and the same long-double-rounded twiddles as the
 // oracle's radix-2 FFT, so the transform is reproducible bit for bit.
 #include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
 #include <stdint.h>
 
 #include "kernels.h"
@@ -162,10 +165,21 @@ size_t qift_smem_bytes(uint32_t P, uint32_t T, int dtype) {
   return (size_t)(1u << P) * T * (dtype == QPE_C128 ? sizeof(double2) : sizeof(float2));
 }
 
+// Only ever raises the limit (per device and type), so that registers of
+// different sizes can be transformed in any order.
 cudaError_t configure_qift_kernels(int dtype, size_t smem) {
-  if (dtype == QPE_C128)
-    return cudaFuncSetAttribute(k_qift<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  return cudaFuncSetAttribute(k_qift<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, size_t> granted;  // (device, dtype) -> bytes
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& g = granted[{dev, dtype}];
+  if (smem <= g) return cudaSuccess;
+  const cudaError_t e =
+      dtype == QPE_C128 ? cudaFuncSetAttribute(k_qift<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                        : cudaFuncSetAttribute(k_qift<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) g = smem;
+  return e;
 }
 
 cudaError_t launch_qift(void* state, uint64_t ld, uint32_t P, const void* tw, double norm, double* partial,

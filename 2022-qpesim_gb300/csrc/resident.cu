@@ -13,7 +13,9 @@
 // A barrier (__syncthreads for K = 1, the cluster barrier otherwise) closes
 // every pass. After a power each CTA copies its rows to block k of the register
 // in global memory (the copy of cpp/time_evolution_over_terms.hpp:130-132, taken
-// after the power), so block k = U^k block 0. No thread waits on a flag: the
+// after the power), so block k = U^k block 0. In place (time_evolve_iqpe, :141-155)
+// the CTA loads block `first`, applies last - first powers and writes block
+// `first` after each. No thread waits on a flag: the
 // only synchronisation is the hardware barrier, reached the same number of
 // times by every CTA of the cluster.
 #include <cooperative_groups.h>
@@ -60,9 +62,9 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
     return cta_ptr(blk, r, K) + (size_t)(a - r * Rk) * Cb + b;
   };
 
-  // Block first - 1 into shared memory.
+  // Block first - 1 (block first when evolving in place) into shared memory.
   {
-    const C2* src = gstate + (uint64_t)(I.first - 1) * ld + (uint64_t)row0 * Cb;
+    const C2* src = gstate + (uint64_t)(I.in_place ? I.first : I.first - 1) * ld + (uint64_t)row0 * Cb;
     for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) blk[i] = src[i];
   }
   barrier();
@@ -161,8 +163,8 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
       barrier();
     }
     }
-    // Snapshot of this CTA's rows into block k.
-    C2* dst = gstate + (uint64_t)k * ld + (uint64_t)row0 * Cb;
+    // Snapshot of this CTA's rows into block k (block first when in place).
+    C2* dst = gstate + (uint64_t)(I.in_place ? I.first : k) * ld + (uint64_t)row0 * Cb;
     for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) dst[i] = blk[i];
     barrier();
   }

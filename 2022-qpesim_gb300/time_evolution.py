@@ -35,6 +35,21 @@ def time_evolve_over_terms(state_vector, hamiltonian: Hamiltonian, precision: in
     return complex(0.0)  # the reference returns an unset std::complex (:98, :138)
 
 
+def time_evolve_iqpe(state_vector, hamiltonian: Hamiltonian, num_of_applications: int, device: int = 0) -> None:
+    """The reference's time_evolve_iqpe (cpp/time_evolution_over_terms.hpp:141-155):
+    block 1 of `state_vector` receives num_of_applications sweeps of U in the term
+    order of applyUnitary (:174-372), in place; no block is copied."""
+    M, e = hamiltonian.num_orbitals(), hamiltonian.num_occupied()
+    ld = math.comb(M, e) ** 2
+    a = np.asarray(state_vector)
+    if a.dtype != np.complex128 or not a.flags.c_contiguous or a.size % ld or a.size < 2 * ld:
+        raise ValueError("state_vector must be a contiguous complex128 array of 2^precision * C(M, e)^2, precision >= 1")
+    precision = (a.size // ld).bit_length() - 1
+    args, keep = N.seg_args(hamiltonian.segmented_terms())
+    N.check(N.lib().qpe_time_evolve_iqpe(N.context(device), M, e, precision, *args, int(num_of_applications),
+                                         a.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))))
+
+
 def plan_program(seg: dict, num_orbitals: int, n_alpha: int, n_beta: int, trotter_order: int = 1,
                  steps: int = 1) -> dict:
     """Host-only planning of a Program (qpe_program_plan): op, pass and update counts."""
@@ -49,10 +64,12 @@ class Program:
 
     trotter_order 2 applies a forward and a reversed sweep per step; pass
     coefficients computed at half the step for a symmetric product. steps is the
-    number of Trotter steps per controlled power. (1, 1) is the reference."""
+    number of Trotter steps per controlled power. (1, 1) is the reference.
+    apply_unitary_order builds the sweep in applyUnitary's term order (the
+    iterative variant) instead of applyUnitary_reordered's."""
 
     def __init__(self, hamiltonian_or_terms, num_orbitals=None, n_alpha=None, n_beta=None, trotter_order=1,
-                 steps=1, device=0):
+                 steps=1, device=0, apply_unitary_order=False):
         if isinstance(hamiltonian_or_terms, Hamiltonian):
             h = hamiltonian_or_terms
             seg = h.segmented_terms()
@@ -67,7 +84,9 @@ class Program:
         args, keep = N.seg_args(seg)
         h = C.c_void_p()
         N.check(self._lib.qpe_program_create(N.context(device), self.num_orbitals, self.n_alpha, self.n_beta, *args,
-                                             int(trotter_order), int(steps), C.byref(h)))
+                                             int(trotter_order) | (N.QPE_PROGRAM_APPLY_UNITARY_ORDER
+                                                                   if apply_unitary_order else 0),
+                                             int(steps), C.byref(h)))
         self._h = h
         info = N.ProgramInfo()
         N.check(self._lib.qpe_program_get_info(h, C.byref(info)))
@@ -125,7 +144,16 @@ class DeviceState:
         memory, 2 a cluster of cluster_size CTAs (0: smallest that fits), 3
         global-memory tile passes. fp64_contract allows FMAs in complex128
         (within 1e-12 of the reference instead of bit-identical)."""
-        opts = N.EvolveOpts(strategy, first_power, last_power, cluster_size, 1 if fp64_contract else 0)
+        opts = N.EvolveOpts(strategy, first_power, last_power, cluster_size,
+                            N.QPE_EVOLVE_FP64_CONTRACT if fp64_contract else 0, 0)
+        N.check(self._lib.qpe_evolve(self._h, program._h, C.byref(opts)))
+
+    def evolve_in_place(self, program: Program, block: int = 1, repeats: int = 1, strategy: int = 0,
+                        cluster_size: int = 0, fp64_contract: bool = False) -> None:
+        """Applies the program's power `repeats` times to block `block` in place
+        (time_evolve_iqpe's evolution with block = 1)."""
+        flags = N.QPE_EVOLVE_IN_PLACE | (N.QPE_EVOLVE_FP64_CONTRACT if fp64_contract else 0)
+        opts = N.EvolveOpts(strategy, block, 0, cluster_size, flags, repeats)
         N.check(self._lib.qpe_evolve(self._h, program._h, C.byref(opts)))
 
     def qift(self) -> None:

@@ -52,6 +52,17 @@ WORKLOADS["batched-256"] = dict(batch=True, count=256, sizes=(12, 14, 16, 18, 20
                                      "(odd N split ceil/floor over the spins), 6 ancilla qubits, complex64 with FP64 "
                                      "coefficients and histograms, 1st-order Trotter dt=0.05, Hartree-Fock starts, "
                                      "one graph launch per step")
+# BASELINE configs[2]: the precision form, one large instance in complex64.
+WORKLOADS["precision-n24"] = dict(n=24, N=12, P=8, dt=0.05, order=1, steps=1, dtype="c64", seed=0, check_c128=True,
+                                  desc="Precision form: n=24, N=12 (853,776 amplitudes per block in the reference's "
+                                       "Na=Nb layout), 8 ancilla qubits, complex64 state with FP64 coefficients, "
+                                       "block norms and histogram, 1st-order Trotter dt=0.05, Hartree-Fock start; "
+                                       "error stated against a complex128 run of the same program")
+# A 32-instance draw of the batching form's distribution: the case the batched
+# kernels are profiled on (same shapes per class, fewer members per launch).
+WORKLOADS["batched-32"] = dict(WORKLOADS["batched-256"], count=32,
+                               desc="Batching form, 32-instance draw (profiling case): n uniform in "
+                                    "{12,14,16,18,20}, N=n/2, 6 ancilla qubits, complex64, dt=0.05")
 DEFAULT_WORKLOAD = "plain-n16"
 
 
@@ -189,6 +200,8 @@ def run_ours(args, w, rank, ws, local):
     prog = q.Program(seg, M, e, e, trotter_order=w["order"], steps=w["steps"], device=local)
     st = q.DeviceState(M, e, e, P, dtype=dtype, device=local)
     npow = (1 << P) - 1
+    if args.powers:  # profiling runs: the first `powers` controlled powers only
+        npow = min(npow, args.powers)
     touches_step = prog.touches_per_power * npow
     block0 = q.hf_block0(st.c_alpha, st.c_beta, P, dtype)
     ctx = N.context(local)
@@ -196,7 +209,7 @@ def run_ours(args, w, rank, ws, local):
     lib = N.lib()
 
     def evolve():
-        st.evolve(prog, strategy=args.strategy, cluster_size=args.cluster)
+        st.evolve(prog, 1, 1 + npow, strategy=args.strategy, cluster_size=args.cluster)
 
     def step():
         evolve()
@@ -290,11 +303,48 @@ def run_ours(args, w, rank, ws, local):
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if args.powers:
+        line["config"]["powers_evolved"] = npow
+    if w.get("check_c128"):
+        line["precision_check"] = precision_check(q, w, seg, st, prog, block0, local)
     if rank == 0 and not args.no_cpu_baseline:
         rate, threads, sample = cpu_baseline(q, w, seg)
         line["cpu_baseline"] = {"value": rate, "unit": "touches/s", "cores": threads, "kind": "port",
                                 "sample": sample}
     return line
+
+
+def precision_check(q, w, seg, st, prog, block0, device):
+    """The complex64 register against a complex128 run of the same program (after
+    the timed steps, outside the timing): amplitude error after the evolution, the
+    phase histogram after the QIFT, and the phase / energy estimates read from
+    each (FP64 readout on both)."""
+    M, e, P = w["n"] // 2, w["N"] // 2, w["P"]
+    ref = q.DeviceState(M, e, e, P, dtype=np.complex128, device=device)
+    ref.upload(block0.astype(np.complex128))
+    ref.evolve(prog)
+    st.upload(block0)
+    st.evolve(prog)
+    norms64, norms128 = st.block_norms(), ref.block_norms()
+    a64 = st.download().astype(np.complex128)
+    a128 = ref.download()
+    amp_err = float(np.max(np.abs(a64 - a128)))
+    rel_l2 = float(np.linalg.norm(a64 - a128) / np.linalg.norm(a128))
+    del a64, a128
+    st.qift()
+    ref.qift()
+    p64, p128 = st.phase_probs(), ref.phase_probs()
+    ph64, ph128 = q.subbin_phase(p64), q.subbin_phase(p128)
+    return {"against": "complex128 run of the same program on the GPU (bit-identical to the FP64 oracle "
+                       "at the parity sizes)",
+            "max_abs_amplitude_error": amp_err, "relative_l2_error": rel_l2,
+            "max_block_norm_drift_c64": float(np.max(np.abs(norms64 - norms64[0]))),
+            "max_block_norm_drift_c128": float(np.max(np.abs(norms128 - norms128[0]))),
+            "histogram_l1_error": float(np.sum(np.abs(p64 - p128))),
+            "argmax_bin": [int(np.argmax(p64)), int(np.argmax(p128))],
+            "reference_phase_estimate": [q.reference_phase(p64), q.reference_phase(p128)],
+            "subbin_phase_estimate": [ph64, ph128], "subbin_phase_error": abs(ph64 - ph128),
+            "energy_error_ha": abs(q.phase_to_energy(ph64, w["dt"]) - q.phase_to_energy(ph128, w["dt"]))}
 
 
 def batch_instances(w, rank=0):
@@ -378,6 +428,7 @@ def run_batch(args, w, rank, ws, local):
     for _ in range(args.warmup):
         upload_all(b0)
         bt.run()
+    info = bt.info  # the launch count is known once the graph exists
     barrier(ws)
     clocks = Clocks()
     clocks.start()
@@ -499,6 +550,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--strategy", type=int, default=0, help="0 auto, 1 one-CTA resident, 2 cluster, 3 tiled")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per cluster for --strategy 2 (0: smallest)")
+    ap.add_argument("--powers", type=int, default=0,
+                    help="evolve only the first K controlled powers (profiling runs; not a workload's figure)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

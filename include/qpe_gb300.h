@@ -131,6 +131,16 @@ int qpe_time_evolve_over_terms(qpe_context* ctx, uint32_t num_orbitals, uint32_t
                                size_t n_pqqp, const qpe_term* pqqr, size_t n_pqqr,
                                const qpe_term* pqrs, size_t n_pqrs, double* state);
 
+/* Replaces time_evolve_iqpe(StateVector&, Hamiltonian&, unsigned num_of_applications)
+ * (cpp/time_evolution_over_terms.hpp:141-155): block 1 of `state` (2^precision
+ * blocks, precision >= 1) receives num_of_applications sweeps of applyUnitary
+ * (:174-372) in place; the other blocks are left as they are. */
+int qpe_time_evolve_iqpe(qpe_context* ctx, uint32_t num_orbitals, uint32_t num_occupied, uint32_t precision,
+                         const qpe_term* pp, size_t n_pp, const qpe_term* pq, size_t n_pq,
+                         const qpe_term* pqqp, size_t n_pqqp, const qpe_term* pqqr, size_t n_pqqr,
+                         const qpe_term* pqrs, size_t n_pqrs, uint32_t num_of_applications,
+                         double* state);
+
 /* Replaces StateVector::qift() (cpp/state_vector.hpp:115-179): in-place forward
  * DFT (sign -1) of length 2^precision along the ancilla axis (stride ld, ld
  * transforms), then division by sqrt(2^precision). */
@@ -157,6 +167,12 @@ typedef struct qpe_program_info {
   uint32_t num_passes_per_power; /* tile passes (kernel launches) per controlled power */
   uint32_t reserved;
 } qpe_program_info;
+
+/* Term order, or-ed into trotter_order of qpe_program_create / qpe_program_plan:
+ * the order of applyUnitary (cpp/time_evolution_over_terms.hpp:174-372), used by
+ * time_evolve_iqpe: every pp, then every pq, pqqp, pqqr (none skipped) and pqrs
+ * term, instead of applyUnitary_reordered's pq-with-nested-pqqr order. */
+#define QPE_PROGRAM_APPLY_UNITARY_ORDER 0x100u
 
 /* Builds the application order and the device pair tables for one Hamiltonian.
  * n_alpha == n_beta reproduces the reference; n_alpha != n_beta is an extension
@@ -195,6 +211,12 @@ int qpe_state_zero(qpe_state* st);
  * reference's rounding by a few ulps per update (within 1e-12 of it) instead of
  * being bit-identical, for about a third fewer FP64 instructions. */
 #define QPE_EVOLVE_FP64_CONTRACT 1u
+/* time_evolve_iqpe (cpp/time_evolution_over_terms.hpp:141-155): block first_power is
+ * evolved in place, `repeats` times (0 = once), with no copy from the block before
+ * it; last_power is ignored. With a program built in the applyUnitary term order
+ * (QPE_PROGRAM_APPLY_UNITARY_ORDER) and first_power = 1 this is the reference's
+ * iterative-QPE evolution. */
+#define QPE_EVOLVE_IN_PLACE 2u
 
 typedef struct qpe_evolve_opts {
   uint32_t strategy;     /* QPE_STRATEGY_* */
@@ -202,6 +224,7 @@ typedef struct qpe_evolve_opts {
   uint32_t last_power;
   uint32_t cluster_size; /* QPE_STRATEGY_CLUSTER: CTAs per cluster (0 = auto) */
   uint32_t flags;        /* QPE_EVOLVE_* */
+  uint32_t repeats;      /* QPE_EVOLVE_IN_PLACE: applications of the power (0 = 1) */
 } qpe_evolve_opts;
 
 /* block_k <- U * block_{k-1} for k = 1 .. 2^P - 1 on the device (opts may be NULL). */

@@ -5,7 +5,8 @@
 // from the caller's Hamiltonian exactly as the reference reads them
 // (PrintIndexedSegmentedHamiltonianTerms and the *_term coefficient getters, at
 // the Hamiltonian's timestep), and the library applies them in the order of
-// applyUnitary_reordered (:374-562) to every controlled power on the GPU.
+// applyUnitary_reordered (:374-562) to every controlled power on the GPU. The
+// iterative variant time_evolve_iqpe (:141-155) is forwarded the same way.
 // A failing call throws a const char* with the library's message, the way the
 // reference reports errors.
 //
@@ -95,6 +96,25 @@ inline std::complex<double> time_evolve_over_terms(StateVector& state_vector, Ha
       T.seg[QPE_TERM_PQRS].size(), reinterpret_cast<double*>(state_vector.data()));
   if (rc != QPE_OK) throw qpe_last_error();
   return std::complex<double>();
+}
+
+// time_evolve_iqpe (:141-155): block 1 evolved in place, num_of_applications
+// sweeps in applyUnitary's term order (:174-372).
+inline void time_evolve_iqpe(StateVector& state_vector, Hamiltonian& hamiltonian, unsigned num_of_applications) {
+  qpesim_gb300::SegmentedTerms T = qpesim_gb300::collect_terms(hamiltonian);
+  auto ptr = [&](int k) { return T.seg[k].empty() ? nullptr : T.seg[k].data(); };
+  // The register's precision from its size: 2^precision blocks of C(M, e)^2.
+  uint64_t c = 1;
+  for (unsigned i = 1; i <= hamiltonian.num_occupied(); ++i)
+    c = c * (hamiltonian.num_orbitals() - hamiltonian.num_occupied() + i) / i;
+  unsigned precision = 0;
+  while ((c * c << (precision + 1)) <= state_vector.size()) ++precision;
+  int rc = qpe_time_evolve_iqpe(
+      qpesim_gb300::default_context(), hamiltonian.num_orbitals(), hamiltonian.num_occupied(), precision,
+      ptr(QPE_TERM_PP), T.seg[QPE_TERM_PP].size(), ptr(QPE_TERM_PQ), T.seg[QPE_TERM_PQ].size(), ptr(QPE_TERM_PQQP), T.seg[QPE_TERM_PQQP].size(), ptr(QPE_TERM_PQQR),
+      T.seg[QPE_TERM_PQQR].size(), ptr(QPE_TERM_PQRS), T.seg[QPE_TERM_PQRS].size(), num_of_applications,
+      reinterpret_cast<double*>(state_vector.data()));
+  if (rc != QPE_OK) throw qpe_last_error();
 }
 
 #endif  // TIME_EVOLUTION_MANUAL_HPP

@@ -91,6 +91,10 @@ class Oracle:
         L.orc_time_evolve.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_uint, P, C.c_size_t, P, C.c_size_t, P,
                                       C.c_size_t, P, C.c_size_t, P, C.c_size_t, C.c_uint, C.c_uint, C.c_uint,
                                       C.c_uint, C.POINTER(C.c_double)]
+        L.orc_time_evolve_iqpe.restype = C.c_int
+        L.orc_time_evolve_iqpe.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_uint, P, C.c_size_t, P, C.c_size_t, P,
+                                           C.c_size_t, P, C.c_size_t, P, C.c_size_t, C.c_uint,
+                                           C.POINTER(C.c_double)]
         L.orc_qift.restype = C.c_int
         L.orc_qift.argtypes = [C.c_uint, C.c_uint64, C.POINTER(C.c_double)]
         L.orc_identify_phase_amplitudes.restype = C.c_int
@@ -134,6 +138,18 @@ class Oracle:
                                       state.view(np.float64).ctypes.data_as(C.POINTER(C.c_double)))
         if rc:
             raise RuntimeError(f"orc_time_evolve failed: {rc}")
+        return state
+
+    def time_evolve_iqpe(self, M, na, nb, P, seg, state, applications):
+        """time_evolve_iqpe: block 1 of `state` evolved in place (applyUnitary order)."""
+        assert state.dtype == np.complex128 and state.flags.c_contiguous
+        args = []
+        for k in ("pp", "pq", "pqqp", "pqqr", "pqrs"):
+            args += list(terms_ptr(seg.get(k)))
+        rc = self.lib.orc_time_evolve_iqpe(M, na, nb, P, *args, applications,
+                                           state.view(np.float64).ctypes.data_as(C.POINTER(C.c_double)))
+        if rc:
+            raise RuntimeError(f"orc_time_evolve_iqpe failed: {rc}")
         return state
 
     def qift(self, P, ld, state):
@@ -191,6 +207,7 @@ class Reference:
         L.ref_segment_terms.restype = C.c_size_t
         L.ref_segment_terms.argtypes = [C.c_void_p, C.c_int, C.POINTER(QpeTerm), C.POINTER(C.c_double), C.c_size_t]
         L.ref_time_evolve.argtypes = [C.c_void_p, C.c_uint, C.POINTER(C.c_double)]
+        L.ref_time_evolve_iqpe.argtypes = [C.c_void_p, C.c_uint, C.POINTER(C.c_double), C.c_uint]
         L.ref_time_steps.restype = C.c_double
         L.ref_time_steps.argtypes = [C.c_void_p, C.c_uint, C.POINTER(C.c_double), C.c_uint]
         L.ref_qift.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.POINTER(C.c_double)]
@@ -251,6 +268,11 @@ class Reference:
 
     def time_evolve(self, h, P, state):
         self.lib.ref_time_evolve(h, P, state.view(np.float64).ctypes.data_as(C.POINTER(C.c_double)))
+        return state
+
+    def time_evolve_iqpe(self, h, P, state, applications):
+        self.lib.ref_time_evolve_iqpe(h, P, state.view(np.float64).ctypes.data_as(C.POINTER(C.c_double)),
+                                      applications)
         return state
 
     def time_steps(self, h, P, state, nsteps):

@@ -411,6 +411,16 @@ static void sweep(cplx* blk, const Geom& g, const Terms& T, bool reversed) {
   }
 }
 
+// applyUnitary (:174-372), the order of the iterative variant: every pp, every
+// pq, every pqqp, every pqqr (no nesting and no skipping), every pqrs.
+static void sweep_apply_unitary(cplx* blk, const Geom& g, const Terms& T) {
+  for (size_t i = 0; i < T.npp; ++i) apply_pp(blk, g, T.pp[i]);
+  for (size_t i = 0; i < T.npq; ++i) apply_pq(blk, g, T.pq[i]);
+  for (size_t i = 0; i < T.npqqp; ++i) apply_pqqp(blk, g, T.pqqp[i]);
+  for (size_t i = 0; i < T.npqqr; ++i) apply_pqqr(blk, g, T.pqqr[i]);
+  for (size_t i = 0; i < T.npqrs; ++i) apply_pqrs(blk, g, T.pqrs[i]);
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -462,6 +472,20 @@ int orc_time_evolve(unsigned M, unsigned ea, unsigned eb, unsigned P, const qpe_
       if (order == 2) sweep(blk, g, T, true);
     }
   }
+  return QPE_OK;
+}
+
+// time_evolve_iqpe (:141-155): block 1 of the register, in place, receives
+// `applications` sweeps of applyUnitary(..., exp = 1); no block is copied.
+int orc_time_evolve_iqpe(unsigned M, unsigned ea, unsigned eb, unsigned P, const qpe_term* pp, size_t npp,
+                         const qpe_term* pq, size_t npq, const qpe_term* pqqp, size_t npqqp, const qpe_term* pqqr,
+                         size_t npqqr, const qpe_term* pqrs, size_t npqrs, unsigned applications, double* state) {
+  if (M == 0 || M > 31 || ea > M || eb > M || P == 0 || P > 30) return QPE_ERR_INVALID;
+  Geom g{M, ea, eb, nck((int)M, (int)ea), nck((int)M, (int)eb), 0};
+  g.block = g.Ca * g.Cb;
+  Terms T{pp, pq, pqqp, pqqr, pqrs, npp, npq, npqqp, npqqr, npqrs};
+  cplx* blk = reinterpret_cast<cplx*>(state) + g.block;
+  for (unsigned i = 0; i < applications; ++i) sweep_apply_unitary(blk, g, T);
   return QPE_OK;
 }
 

@@ -183,6 +183,17 @@ int ref_time_evolve(void* hv, unsigned P, double* state) {
   return 0;
 }
 
+// time_evolve_iqpe on a StateVector holding `state` (all 2^P C^2 values, in and out).
+int ref_time_evolve_iqpe(void* hv, unsigned P, double* state, unsigned applications) {
+  Quiet q;
+  auto* h = static_cast<Hamiltonian*>(hv);
+  StateVector sv(P, h->num_orbitals(), h->num_occupied());
+  std::memcpy(sv.data(), state, sv.size() * sizeof(std::complex<double>));
+  time_evolve_iqpe(sv, *h, applications);
+  std::memcpy(state, sv.data(), sv.size() * sizeof(std::complex<double>));
+  return 0;
+}
+
 // Seconds per call of applyUnitary_reordered after the setup of
 // time_evolve_over_terms (used to time the reference on a bounded sample).
 double ref_time_steps(void* hv, unsigned P, double* state, unsigned nsteps) {

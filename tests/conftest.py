@@ -48,7 +48,7 @@ def load_golden(name):
 
 def golden_segments(z, prefix=""):
     """kind -> TERM_DTYPE array stored by make_golden.py."""
-    from qpesim_gb300 import TERM_DTYPE  # noqa: E402
+    TERM_DTYPE = graft.load_package().TERM_DTYPE
     out = {}
     for k in ("pp", "pq", "pqqp", "pqqr", "pqrs"):
         raw = z[prefix + k]

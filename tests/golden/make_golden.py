@@ -9,6 +9,8 @@ embedded doctests, and stores the results as small .npz / .json files:
   evolve_*.npz                  block 0, the evolved register, the QIFT output and
                                 the phase histogram of time_evolve_over_terms / qift /
                                 IdentifyPhaseAmplitudes
+  iqpe_*.npz                    the register before and after time_evolve_iqpe
+                                (block 1 evolved in place, applyUnitary order)
   discover.npz                  run tables of the five discover*_BVs routines
   swaps.npz                     OffsetComputer rank_with_swap / rank_with_double_swap
   broombridge_*.npz             terms and block 0 from IngestBroombridge on files
@@ -43,6 +45,7 @@ EVOLVE_CASES = [
     (10, 2, 2, 0.1, 7),
 ]
 TERM_CASES = [(8, 4, 0.1, 0), (12, 6, 0.05, 3), (16, 8, 0.05, 11), (6, 2, 1.0, 5)]
+IQPE_CASES = [(6, 2, 1, 0.2, 2, 4), (8, 4, 2, 0.1, 3, 3), (10, 6, 1, 0.05, 5, 2), (12, 6, 1, 0.05, 6, 1)]
 SINGLE_TERM_FILES = ["PP.yml", "PQ.yml", "PQQP.yml", "PQQR.yml", "PQRS.yml", "h4_sto6g_0.100.yaml"]
 
 
@@ -87,6 +90,24 @@ def main():
         probs = ref.identify_phase_amplitudes(P, M, e, state)
         np.savez_compressed(HERE / f"evolve_n{n}_N{N}_P{P}_s{seed}.npz", n=n, N=N, P=P, dt=dt, seed=seed,
                             block0=block0, evolved=evolved, qift=state, probs=probs, **seg_arrays(seg, raw))
+        ref.destroy(h)
+
+    # time_evolve_iqpe: block 1 (a seeded random state) evolved in place.
+    for n, N, P, dt, seed, apps in IQPE_CASES:
+        M, e = n // 2, N // 2
+        it = q.synthetic_integrals(n, seed)
+        h = ref.hamiltonian(M, e, it.one_body, it.two_body, dt)
+        seg, raw = ref.segments(h)
+        C = ref.nchoosek(M, e)
+        rng = np.random.default_rng(seed)
+        state = np.zeros((1 << P) * C * C, np.complex128)
+        state[0] = 1.0
+        state[C * C:2 * C * C] = rng.standard_normal(C * C) + 1j * rng.standard_normal(C * C)
+        state[C * C:2 * C * C] /= np.linalg.norm(state[C * C:2 * C * C])
+        before = state.copy()
+        ref.time_evolve_iqpe(h, P, state, apps)
+        np.savez_compressed(HERE / f"iqpe_n{n}_N{N}_P{P}_a{apps}_s{seed}.npz", n=n, N=N, P=P, dt=dt, seed=seed,
+                            applications=apps, before=before, after=state, **seg_arrays(seg, raw))
         ref.destroy(h)
 
     # discover tables

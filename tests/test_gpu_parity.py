@@ -12,7 +12,7 @@ import math
 import numpy as np
 import pytest
 
-from conftest import evolve_cases, golden_segments, load_golden
+from conftest import GOLDEN, evolve_cases, golden_segments, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -321,3 +321,86 @@ def test_batch_matches_oracle_per_instance(gpu, orc, dtype):
                 assert np.abs(got - ref).max() < 2e-5, i
             np.testing.assert_allclose(bt.phase_probs(i), orc.identify_phase_amplitudes(P, ld, ref), rtol=1e-4,
                                        atol=1e-6)
+
+
+@pytest.mark.parametrize("name", sorted(p.name for p in GOLDEN.glob("iqpe_*.npz")))
+@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 2), (3, 0), (0, 0)])
+def test_iqpe_golden(gpu, name, strategy, cluster):
+    """time_evolve_iqpe (cpp/time_evolution_over_terms.hpp:141-155): block 1 in
+    place, applyUnitary's term order, against the reference's own output, through
+    the device-resident form under every strategy and through the host call."""
+    q = gpu
+    z = load_golden(name)
+    n, N, P, apps = int(z["n"]), int(z["N"]), int(z["P"]), int(z["applications"])
+    M, e = n // 2, N // 2
+    seg = golden_segments(z)
+    prog = q.Program(seg, M, e, e, apply_unitary_order=True)
+    st = q.DeviceState(M, e, e, P)
+    st.upload(z["before"])
+    st.evolve_in_place(prog, block=1, repeats=apps, strategy=strategy, cluster_size=cluster)
+    np.testing.assert_allclose(st.download(), z["after"], rtol=0, atol=1e-13)
+    if strategy == 0:
+        h = q.Hamiltonian.from_integrals(q.synthetic_integrals(n, int(z["seed"])), e, float(z["dt"]))
+        sv = z["before"].copy()
+        q.time_evolve_iqpe(sv, h, apps)
+        np.testing.assert_allclose(sv, z["after"], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("strategy", [1, 3])
+def test_iqpe_bit_identical_to_oracle(gpu, orc, strategy):
+    q = gpu
+    M, e, P, apps = 6, 3, 2, 3
+    seg = _seg(q, 12, 6, 41, 0.08)
+    rng = np.random.default_rng(41)
+    st = q.DeviceState(M, e, e, P)
+    reg = (rng.standard_normal(st.size) + 1j * rng.standard_normal(st.size)) / np.sqrt(st.size)
+    st.upload(reg)
+    st.evolve_in_place(q.Program(seg, M, e, e, apply_unitary_order=True), 1, apps, strategy=strategy)
+    orc.time_evolve_iqpe(M, e, e, P, seg, reg, apps)
+    assert np.array_equal(st.download(), reg)
+
+
+@pytest.mark.parametrize("strategy,order,steps", [(1, 1, 1), (2, 2, 2), (3, 2, 1)])
+def test_in_place_repeats_equal_powers(gpu, strategy, order, steps):
+    """r in-place applications to block 1 holding block 0 give block r of the
+    ordinary controlled-power evolution, bit for bit, in any strategy."""
+    q = gpu
+    M, na, nb, P, r = 5, 2, 3, 3, 5
+    seg = _seg(q, 10, 6, 52, 0.06)
+    prog = q.Program(seg, M, na, nb, trotter_order=order, steps=steps)
+    a = q.DeviceState(M, na, nb, P)
+    b = q.DeviceState(M, na, nb, P)
+    rng = np.random.default_rng(52)
+    b0 = (rng.standard_normal(a.ld) + 1j * rng.standard_normal(a.ld)) / np.sqrt(2 * a.ld)
+    a.upload(b0)
+    a.evolve(prog, strategy=strategy, cluster_size=2 if strategy == 2 else 0)
+    reg = np.zeros(b.size, np.complex128)
+    reg[:b.ld] = b0
+    reg[b.ld:2 * b.ld] = b0
+    b.upload(reg)
+    b.evolve_in_place(prog, 1, r, strategy=strategy, cluster_size=2 if strategy == 2 else 0)
+    got = b.download()
+    assert np.array_equal(got[b.ld:2 * b.ld], a.download()[r * b.ld:(r + 1) * b.ld])
+    assert np.array_equal(got[2 * b.ld:], reg[2 * b.ld:])
+
+
+def test_autotune_leaves_register_unchanged(gpu):
+    """The autotuner's trial powers write block 1; it is put back, so a partial
+    range or an in-place call that triggers tuning sees the register it was given."""
+    q = gpu
+    seg = _seg(q, 12, 6, 61, 0.05)
+    prog = q.Program(seg, 6, 3, 3)
+    st = q.DeviceState(6, 3, 3, 3)
+    rng = np.random.default_rng(61)
+    reg = (rng.standard_normal(st.size) + 1j * rng.standard_normal(st.size)) / np.sqrt(st.size)
+    st.upload(reg)
+    st.evolve(prog, 5, 6)  # first use: tunes, then evolves block 5 from block 4
+    got = st.download()
+    assert np.array_equal(np.delete(got.reshape(8, -1), 5, axis=0), np.delete(reg.reshape(8, -1), 5, axis=0))
+    prog2 = q.Program(seg, 6, 3, 3, apply_unitary_order=True)
+    st.upload(reg)
+    st.evolve_in_place(prog2, 1, 2)  # tunes on prog2 first
+    ref = q.DeviceState(6, 3, 3, 3)
+    ref.upload(reg)
+    ref.evolve_in_place(prog2, 1, 2, strategy=3)
+    assert np.array_equal(st.download(), ref.download())

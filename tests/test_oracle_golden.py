@@ -27,6 +27,19 @@ def test_oracle_evolution_matches_reference(orc, name):
     np.testing.assert_allclose(orc.identify_phase_amplitudes(P, ld, state), z["probs"], rtol=1e-12, atol=1e-15)
 
 
+@pytest.mark.parametrize("name", sorted(p.name for p in GOLDEN.glob("iqpe_*.npz")))
+def test_oracle_iqpe_matches_reference(orc, name):
+    """time_evolve_iqpe (cpp/time_evolution_over_terms.hpp:141-155): block 1 in
+    place, applyUnitary's term order, no copy of block 0."""
+    z = load_golden(name)
+    n, N, P = int(z["n"]), int(z["N"]), int(z["P"])
+    state = z["before"].copy()
+    orc.time_evolve_iqpe(n // 2, N // 2, N // 2, P, golden_segments(z), state, int(z["applications"]))
+    np.testing.assert_allclose(state, z["after"], rtol=0, atol=TOL)
+    ld = len(state) >> P
+    assert np.array_equal(state[:ld], z["before"][:ld]) and np.array_equal(state[2 * ld:], z["before"][2 * ld:])
+
+
 def test_oracle_discover_tables(orc):
     z = load_golden("discover.npz")
     rows, tabs = z["rows"], z["tables"]
