@@ -98,7 +98,23 @@ PROTOTYPES = {
     "qpe_state_qift": (C.c_int, [_vp]),
     "qpe_state_phase_probs": (C.c_int, [_vp, _PD]),
     "qpe_state_block_norms": (C.c_int, [_vp, _PD]),
+    "qpe_state_last_strategy": (C.c_int, [_vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     # host-side term compiler
+    # learned initial-state model
+    "qpe_mlp_create": (C.c_int, [_vp, C.c_uint32, C.c_uint32, C.c_uint64, C.POINTER(_vp)]),
+    "qpe_mlp_destroy": (C.c_int, [_vp]),
+    "qpe_mlp_num_params": (C.c_int, [_vp, C.POINTER(C.c_uint64)]),
+    "qpe_mlp_get_params": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "qpe_mlp_set_params": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "qpe_mlp_set_data": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                   C.POINTER(C.c_float), C.c_uint64]),
+    "qpe_mlp_train": (C.c_int, [_vp, C.c_uint32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
+    "qpe_mlp_forward": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.c_uint64, C.POINTER(C.c_float)]),
+    "qpe_mlp_gradients": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                    C.POINTER(C.c_float), C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "qpe_mlp_tensor_flops_per_step": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "qpe_gemm_bf16": (C.c_int, [_vp, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint16),
+                                C.POINTER(C.c_uint16), C.POINTER(C.c_float), C.c_uint32]),
     "qpe_ham_create": (C.c_int, [C.POINTER(_vp)]),
     "qpe_ham_destroy": (C.c_int, [_vp]),
     "qpe_ham_add_one_body": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double]),

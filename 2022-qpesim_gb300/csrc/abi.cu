@@ -40,6 +40,7 @@ struct qpe_state {
   uint64_t tuned_prog = 0;
   uint32_t tuned_exact = 1;
   uint32_t tuned_strategy = 0, tuned_cluster = 0;
+  uint32_t last_strategy = 0, last_cluster = 0;
   ~qpe_state() {
     if (graph) cudaGraphExecDestroy(graph);
   }
@@ -159,8 +160,14 @@ PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_opt
   if (stage > smem_optin) throw Error(QPE_ERR_UNSUPPORTED, "block too large for a shared-memory tile");
   uint32_t wpc = 4;
   while (wpc > 1 && stage * wpc > smem_optin) --wpc;
-  pl.warps_per_cta = wpc;
   uint64_t ntiles = pass.type == PASS_COL ? (hp.Cb + W - 1) / W : (pass.type == PASS_ROW ? hp.Ca : pass.mixcount);
+  if (esz == 16) {
+    // complex128 tiles are bound by the SM's FP64 issue rate: spread the tiles
+    // over the SMs first, then stack warps.
+    const uint64_t per_sm = (ntiles + pr->ctx->num_sms - 1) / pr->ctx->num_sms;
+    wpc = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(wpc, per_sm));
+  }
+  pl.warps_per_cta = wpc;
   uint64_t grid = (ntiles + wpc - 1) / wpc;
   const uint64_t cap = (uint64_t)pr->ctx->num_sms * 8;
   if (grid > cap) grid = cap;
@@ -215,7 +222,8 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
     const uint64_t ea = binom((int)hp.M - 2, (int)hp.na - 1), eb = binom((int)hp.M - 2, (int)hp.nb - 1);
     ri.Wr = choose_lines(Rk, wpc, eb ? eb : 1);
     ri.Wc = choose_lines(Cb, (uint64_t)K * wpc, ea ? ea : 1);
-    ri.Wm = choose_lines(mixcount ? mixcount : 1, (uint64_t)K * wpc, ea ? ea : 1);
+    // at most 16 column pairs per tile: a lane's gather column is then fixed
+    ri.Wm = std::min<uint32_t>(16u, choose_lines(mixcount ? mixcount : 1, (uint64_t)K * wpc, ea ? ea : 1));
     uint64_t stage = 0;
     if (K > 1) {
       while (true) {
@@ -379,6 +387,8 @@ static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* 
   const bool exact = st->dtype == QPE_C128 && !(opts && (opts->flags & QPE_EVOLVE_FP64_CONTRACT));
   uint32_t strategy = 0, K = 0;
   choose_strategy(st, pr, opts, exact, strategy, K);
+  st->last_strategy = strategy;
+  st->last_cluster = strategy == QPE_STRATEGY_TILED ? 0 : K;
   if (strategy == QPE_STRATEGY_TILED) {
     evolve_tiled(st, pr, first, last, exact, in_place);
   } else {
@@ -847,7 +857,8 @@ int qpe_evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts
     if (opts && opts->strategy > QPE_STRATEGY_TILED) throw Error(QPE_ERR_INVALID, "unknown strategy");
     if (opts && opts->cluster_size && (opts->cluster_size > 16 || (opts->cluster_size & (opts->cluster_size - 1))))
       throw Error(QPE_ERR_INVALID, "cluster_size must be a power of two <= 16");
-    if (opts && (opts->flags & ~QPE_EVOLVE_FP64_CONTRACT)) throw Error(QPE_ERR_INVALID, "unknown evolve flag");
+    if (opts && (opts->flags & ~(QPE_EVOLVE_FP64_CONTRACT | QPE_EVOLVE_IN_PLACE)))
+      throw Error(QPE_ERR_INVALID, "unknown evolve flag");
     evolve(st, pr, opts);
   });
 }
@@ -868,6 +879,14 @@ int qpe_state_phase_probs(qpe_state* st, double* probs) {
     }
     QPE_CK(cudaMemcpyAsync(probs, st->probs.p, st->N * sizeof(double), cudaMemcpyDeviceToHost, st->ctx->stream));
     QPE_CK(cudaStreamSynchronize(st->ctx->stream));
+  });
+}
+
+int qpe_state_last_strategy(const qpe_state* st, uint32_t* strategy, uint32_t* cluster_size) {
+  return guard([&] {
+    if (!st || !strategy || !cluster_size) throw Error(QPE_ERR_INVALID, "null argument");
+    *strategy = st->last_strategy;
+    *cluster_size = st->last_cluster;
   });
 }
 

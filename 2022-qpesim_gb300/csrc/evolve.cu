@@ -61,14 +61,29 @@ __global__ void k_pass(PassLaunch pl) {
       parb = x.x >> 31;
     }
     const uint32_t nl = (PT == PASS_COL) ? min(W, Cb - b0) : W;  // valid lines
-    for (uint32_t i = lane; i < L * W; i += 32) {
+    // Element i of the stage <-> block offset g(i). Gathers keep kU loads in
+    // flight per lane before their shared-memory stores, so a tile pays the L2
+    // latency once per kU elements rather than once per element.
+    auto goff = [&](uint32_t i) -> uint64_t {
       const uint32_t e = i >> logW, w = i & (W - 1);
-      if (w >= nl) continue;
-      uint64_t g;
-      if (PT == PASS_COL) g = (uint64_t)e * Cb + b0 + w;
-      else if (PT == PASS_ROW) g = (uint64_t)row * Cb + e;
-      else g = (uint64_t)e * Cb + (w ? b10 : b01);
-      st[i] = blk[g];
+      if (PT == PASS_COL) return (uint64_t)e * Cb + b0 + w;
+      if (PT == PASS_ROW) return (uint64_t)row * Cb + e;
+      return (uint64_t)e * Cb + (w ? b10 : b01);
+    };
+    constexpr uint32_t kU = 8;
+    const uint32_t nst = L * W;
+    for (uint32_t base = lane; base < nst; base += 32 * kU) {
+      C2 v[kU];
+#pragma unroll
+      for (uint32_t u = 0; u < kU; ++u) {
+        const uint32_t i = base + 32 * u;
+        if (i < nst && (i & (W - 1)) < nl) v[u] = blk[goff(i)];
+      }
+#pragma unroll
+      for (uint32_t u = 0; u < kU; ++u) {
+        const uint32_t i = base + 32 * u;
+        if (i < nst && (i & (W - 1)) < nl) st[i] = v[u];
+      }
     }
     __syncwarp();
     if (PT == PASS_MIX) {
@@ -84,15 +99,8 @@ __global__ void k_pass(PassLaunch pl) {
       run_line_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, L, lane >> logW, 32 >> logW,
                          active, lstr, [&](uint32_t e) -> C2& { return st[(e << logW) + w]; }, icoef);
     }
-    for (uint32_t i = lane; i < L * W; i += 32) {
-      const uint32_t e = i >> logW, w = i & (W - 1);
-      if (w >= nl) continue;
-      uint64_t g;
-      if (PT == PASS_COL) g = (uint64_t)e * Cb + b0 + w;
-      else if (PT == PASS_ROW) g = (uint64_t)row * Cb + e;
-      else g = (uint64_t)e * Cb + (w ? b10 : b01);
-      blk[g] = st[i];
-    }
+    for (uint32_t i = lane; i < nst; i += 32)
+      if ((i & (W - 1)) < nl) blk[goff(i)] = st[i];
     __syncwarp();
   }
 }

@@ -10,8 +10,10 @@
 //          column-pair tiles are gathered from the cluster's shared memories
 //          (distributed shared memory) into a warp-private stage, processed,
 //          and scattered back.
-// A barrier (__syncthreads for K = 1, the cluster barrier otherwise) closes
-// every pass. After a power each CTA copies its rows to block k of the register
+// Column and column-pair tiles go round-robin over the cluster's CTAs (tile t to
+// CTA t % K), so that a pass with fewer tiles than warps still spreads its FP64
+// work over every SM of the cluster. A barrier (__syncthreads for K = 1, the
+// cluster barrier otherwise) closes every pass. After a power each CTA copies its rows to block k of the register
 // in global memory (the copy of cpp/time_evolution_over_terms.hpp:130-132, taken
 // after the power), so block k = U^k block 0. In place (time_evolve_iqpe, :141-155)
 // the CTA loads block `first`, applies last - first powers and writes block
@@ -33,6 +35,26 @@ template <typename C2>
 __device__ __forceinline__ C2* cta_ptr(C2* local, uint32_t rank, uint32_t K) {
   if (K == 1) return local;
   return cg::this_cluster().map_shared_rank(local, rank);
+}
+
+// Copies elements i = lane, lane + 32, ... < n for which ok(i) holds from
+// *src(i) to *dst(i), U loads in flight per lane before their stores, so that
+// distributed-shared-memory latency is paid once per U elements.
+template <typename V, int U, class Ok, class Src, class Dst>
+__device__ __forceinline__ void warp_copy(uint32_t n, uint32_t lane, Ok ok, Src src, Dst dst) {
+  for (uint32_t base = lane; base < n; base += 32 * U) {
+    V v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t i = base + 32 * u;
+      if (i < n && ok(i)) v[u] = *src(i);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t i = base + 32 * u;
+      if (i < n && ok(i)) *dst(i) = v[u];
+    }
+  }
 }
 
 template <typename R, class A>
@@ -95,7 +117,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
         const uint32_t W = I.Wc, logW = __ffs(W) - 1, w = lane & (W - 1);
         const uint32_t jl = lane >> logW, jstep = 32 >> logW;
         const uint32_t ntiles = (Cb + W - 1) >> logW;
-        const uint32_t gw = rank * wpc + warp, nw = K * wpc;
+        const uint32_t gw = warp * K + rank, nw = K * wpc;  // tile t on CTA t % K
         for (uint32_t tile = gw; tile < ntiles; tile += nw) {
           const uint32_t b0 = tile << logW, c = b0 + w;
           const bool active = c < Cb;
@@ -106,17 +128,14 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
                                [&](uint32_t e) -> C2& { return col[(size_t)e * Cb]; });
           } else {
             const uint32_t nl = min(W, Cb - b0);
-            for (uint32_t i = lane; i < (Ca << logW); i += 32) {
-              const uint32_t e = i >> logW, ww = i & (W - 1);
-              if (ww < nl) stage[i] = *at(e, b0 + ww);
-            }
+            auto ok = [&](uint32_t i) { return (i & (W - 1)) < nl; };
+            auto remote = [&](uint32_t i) { return at(i >> logW, b0 + (i & (W - 1))); };
+            auto local = [&](uint32_t i) { return stage + i; };
+            warp_copy<C2, 4>(Ca << logW, lane, ok, remote, local);
             __syncwarp();
             run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, Ca, jl, jstep, active, lstr,
                                [&](uint32_t e) -> C2& { return stage[(e << logW) + w]; });
-            for (uint32_t i = lane; i < (Ca << logW); i += 32) {
-              const uint32_t e = i >> logW, ww = i & (W - 1);
-              if (ww < nl) *at(e, b0 + ww) = stage[i];
-            }
+            warp_copy<C2, 4>(Ca << logW, lane, ok, local, remote);
             __syncwarp();
           }
         }
@@ -124,7 +143,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
         const uint32_t W = I.Wm, logW = __ffs(W) - 1, w = lane & (W - 1);
         const uint32_t jl = lane >> logW, jstep = 32 >> logW;
         const uint32_t ntiles = (P.mixcount + W - 1) >> logW;
-        const uint32_t gw = rank * wpc + warp, nw = K * wpc;
+        const uint32_t gw = warp * K + rank, nw = K * wpc;  // tile t on CTA t % K
         const uint2* __restrict__ mt = reinterpret_cast<const uint2*>(I.pool + P.mixtab);
         for (uint32_t tile = gw; tile < ntiles; tile += nw) {
           const uint32_t t0 = tile << logW, t = t0 + w;
@@ -138,24 +157,20 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
           } else {
             const uint32_t nl = min(W, P.mixcount - t0);
             const uint32_t n2 = Ca << (logW + 1);
-            for (uint32_t i = lane; i < n2; i += 32) {
-              const uint32_t a = i >> (logW + 1), ww = (i >> 1) & (W - 1), side = i & 1;
-              if (ww < nl) {
-                const uint2 q = __ldg(mt + t0 + ww);
-                stage[i] = *at(a, side ? q.y : (q.x & 0x7fffffffu));
-              }
-            }
+            // lane's column of element i: column-pair (i >> 1) & (W - 1), side i & 1;
+            // with 32 a multiple of 2W it is the same for every i of the lane.
+            const uint32_t mysel = lane & (2 * W - 1);
+            const uint2 myq = ((mysel >> 1) < nl) ? __ldg(mt + t0 + (mysel >> 1)) : make_uint2(0u, 0u);
+            const uint32_t mycol = (mysel & 1) ? myq.y : (myq.x & 0x7fffffffu);
+            auto ok = [&](uint32_t) { return (mysel >> 1) < nl; };
+            auto remote = [&](uint32_t i) { return at(i >> (logW + 1), mycol); };
+            auto local = [&](uint32_t i) { return stage + i; };
+            warp_copy<C2, 4>(n2, lane, ok, remote, local);
             __syncwarp();
             run_mix_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, jl, jstep, active, parb,
                               [&](uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w]; },
                               [&](uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w + 1]; });
-            for (uint32_t i = lane; i < n2; i += 32) {
-              const uint32_t a = i >> (logW + 1), ww = (i >> 1) & (W - 1), side = i & 1;
-              if (ww < nl) {
-                const uint2 q = __ldg(mt + t0 + ww);
-                *at(a, side ? q.y : (q.x & 0x7fffffffu)) = stage[i];
-              }
-            }
+            warp_copy<C2, 4>(n2, lane, ok, local, remote);
             __syncwarp();
           }
         }

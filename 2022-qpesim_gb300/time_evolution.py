@@ -164,6 +164,12 @@ class DeviceState:
         N.check(self._lib.qpe_state_phase_probs(self._h, p.ctypes.data_as(C.POINTER(C.c_double))))
         return p
 
+    def last_strategy(self) -> tuple:
+        """(strategy, cluster size) of the last evolve: 1 resident, 2 cluster, 3 tiled."""
+        s, k = C.c_uint32(), C.c_uint32()
+        N.check(self._lib.qpe_state_last_strategy(self._h, C.byref(s), C.byref(k)))
+        return s.value, k.value
+
     def block_norms(self) -> np.ndarray:
         p = np.zeros(1 << self.precision)
         N.check(self._lib.qpe_state_block_norms(self._h, p.ctypes.data_as(C.POINTER(C.c_double))))

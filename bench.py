@@ -268,7 +268,14 @@ def run_ours(args, w, rank, ws, local):
     achieved = touches_step * bpt / ev_s / 1e9
     peak, peak_kind = peaks()
     info = prog.info
-    launches = args.steps * (npow * (info["num_passes_per_power"] + 2) + 1 + 2 + 1)
+    strat, kc = st.last_strategy()
+    if strat == 3:
+        kernel = "k_pass (evolution tile passes, one launch per pass)"
+        launches = args.steps * (npow * (info["num_passes_per_power"] + 2) + 1 + 2 + 1)
+    else:
+        kernel = f"k_resident (whole evolution in one launch, cluster of {kc} CTA(s))"
+        launches = args.steps * (1 + 2)
+    strategy_name = {1: "resident (one CTA)", 2: f"cluster of {kc} CTAs", 3: "tiled passes"}.get(strat, "?")
     line = {
         "metric": "amplitude-term updates/s per Trotter step",
         "value": value,
@@ -288,15 +295,15 @@ def run_ours(args, w, rank, ws, local):
                    "steps_per_power": w["steps"], "state": w["dtype"], "amps_per_block": st.ld,
                    "blocks": 1 << P, "touches_per_power": prog.touches_per_power,
                    "touches_per_step": touches_step, "l2": "flushed before every timed step",
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"replicas x{ws}", "strategy": strategy_name},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
-                     "kernel": "k_pass (evolution tile passes)",
+                     "kernel": kernel,
                      "fp64": {"achieved_tflops": touches_step * 6 / ev_s / 1e12, "peak_tflops": FP64_PEAK_TFLOPS,
                               "frac": touches_step * 6 / ev_s / 1e12 / FP64_PEAK_TFLOPS,
                               "flops_per_touch": 6}} if w["dtype"] == "c128" else
                     {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": peak_kind, "kernel": "k_pass (evolution tile passes)"},
+                     "traffic": None, "peak_source": peak_kind, "kernel": kernel},
         "e2e": {"value": e2e_value, "unit": "touches/s",
                 "h2d_bytes_per_step": int(st.ld * dtype().itemsize),
                 "d2h_bytes_per_step": int(st.size * dtype().itemsize + (1 << P) * 8)},

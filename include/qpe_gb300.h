@@ -235,6 +235,8 @@ int qpe_state_qift(qpe_state* st);
 int qpe_state_phase_probs(qpe_state* st, double* probs);
 /* Per-block squared norms (2^P doubles, FP64 accumulation). */
 int qpe_state_block_norms(qpe_state* st, double* norms);
+/* Strategy (QPE_STRATEGY_*) and cluster size the last qpe_evolve on this state ran. */
+int qpe_state_last_strategy(const qpe_state* st, uint32_t* strategy, uint32_t* cluster_size);
 
 /* ---- batching form ----------------------------------------------------------------
  * Many Hamiltonians (programs) evolved, transformed and read out by one launch of

@@ -32,3 +32,15 @@ def test_no_device_fails_loudly(q):
     with pytest.raises(q.QpeError) as ei:
         q.OffsetComputer.rank(5)
     assert ei.value.code == 6
+
+
+def test_bf16_helpers_and_mlp_layout(q):
+    import numpy as np
+    import qpesim_gb300.learned_state as L
+    x = np.array([1.0, -2.5, 3.14159, 1e-3, 65504.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -9], np.float32)
+    r = L.round_bf16(x)
+    assert r[0] == 1.0 and r[1] == -2.5 and abs(r[2] - 3.140625) < 1e-7
+    assert r[5] == 1.0  # halfway, ties to even
+    assert r[6] == np.float32(1.0 + 2 ** -7)
+    lay = L.param_layout()
+    assert sum(int(np.prod(s)) for _, s in lay.values()) == 152336
