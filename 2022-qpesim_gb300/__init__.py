@@ -10,6 +10,7 @@ The directory is named 2022-qpesim_gb300, which is not an importable module
 name; __graft_entry__.load_package() registers it as `qpesim_gb300`.
 """
 from . import _native
+from . import learned_state
 from .batching import Batch
 from .hamiltonian import Hamiltonian, SpinIndex
 from .offset_computer import OffsetComputer

@@ -213,6 +213,11 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
   uint32_t mixcount = 0;
   for (const Pass& p : hp.passes)
     if (p.type == PASS_MIX) mixcount = std::max(mixcount, p.mixcount);
+  const size_t meta = resident_meta_bytes((uint32_t)hp.ops.size(), (uint32_t)hp.pool_words,
+                                          (uint32_t)hp.passes.size(), (uint32_t)Ca, (uint32_t)Cb);
+  // First choice: the program's metadata staged in shared memory too; then the
+  // block (and warp stages) alone.
+  for (int with_meta = 1; with_meta >= 0; --with_meta)
   for (uint32_t wpc = 16; wpc >= 4; wpc /= 2) {
     ri = ResidentInstance{};
     ri.Ca = (uint32_t)Ca;
@@ -233,13 +238,15 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
         if (ri.Wm > 1 && 2 * Ca * ri.Wm > Ca * ri.Wc) ri.Wm /= 2;
       }
     }
-    const size_t smem = (size_t)(Rk * Cb * esz + wpc * stage * esz);
+    const size_t head = (size_t)(Rk * Cb * esz + wpc * stage * esz);
+    const size_t smem = with_meta ? ((head + 15) & ~(size_t)15) + meta : head;
     if (smem <= st->ctx->smem_optin) {
       rl = ResidentLaunch{};
       rl.ninst = 1;
       rl.cluster = K;
       rl.warps_per_cta = wpc;
       rl.stage_elems = (uint32_t)stage;
+      rl.meta_smem = (uint32_t)with_meta;
       rl.smem_bytes = smem < 1024 ? 1024 : smem;
       return true;
     }
@@ -260,6 +267,8 @@ static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint3
   ri.strA = pr->strA.as<uint32_t>();
   ri.strB = pr->strB.as<uint32_t>();
   ri.npasses = (uint32_t)pr->hp.passes.size();
+  ri.nops = (uint32_t)pr->hp.ops.size();
+  ri.pool_words = (uint32_t)pr->hp.pool_words;
   ri.first = first;
   ri.last = last;
   ri.steps = pr->hp.steps;

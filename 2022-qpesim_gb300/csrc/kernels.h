@@ -77,6 +77,7 @@ struct ResidentInstance {
   uint32_t rows_per_cta;    // rows owned by each CTA of the cluster
   uint32_t Wc, Wr, Wm;
   uint32_t steps, order;    // Trotter steps per power; 2 = forward + backward sweep
+  uint32_t nops, pool_words;  // sizes of the term descriptors and the index pool
   uint32_t in_place;        // 1: block `first` is loaded, evolved last - first times
                             //    and written back to itself (iterative QPE)
 };
@@ -86,12 +87,15 @@ struct ResidentLaunch {
   uint32_t cluster;               // CTAs per instance (1 = one CTA)
   uint32_t warps_per_cta;
   uint32_t stage_elems;           // per-warp stage (cluster > 1)
+  uint32_t meta_smem;             // 1: term descriptors, index pool, passes and line
+                                  //    strings are staged in every CTA's shared memory
   size_t smem_bytes;
 };
+// Bytes of shared memory the staged program metadata takes (ResidentLaunch::meta_smem).
+size_t resident_meta_bytes(uint32_t nops, uint32_t pool_words, uint32_t npasses, uint32_t Ca, uint32_t Cb);
 cudaError_t launch_resident(const ResidentLaunch& rl, int dtype, int exact, cudaStream_t s);
 // Shared-memory carveout (percent of the maximum) the resident kernel asks for.
 cudaError_t set_resident_carveout(int dtype, int exact, int percent);
-cudaError_t resident_max_cluster(int dtype, uint32_t cluster, uint32_t warps, size_t smem, int* max_clusters);
 
 // ---- QIFT and reductions (qift.cu) ----
 cudaError_t launch_qift(void* state, uint64_t ld, uint32_t P, const void* twiddles, double norm, double* partial,

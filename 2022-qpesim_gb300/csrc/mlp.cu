@@ -273,12 +273,25 @@ __global__ void k_loss(const float* __restrict__ Y, const float* __restrict__ bl
   if (threadIdx.x == 0) atomicAdd(loss, red[0]);
 }
 
-// out[c] = sum over rows r < R of src[r, c] (BF16 -> FP32), c < C.
-__global__ void k_colsum(const bf16* __restrict__ src, uint32_t R, uint32_t C, uint32_t lds, float* __restrict__ out) {
+// Column sums of a BF16 matrix in two fixed-order phases: block b sums rows
+// [256 b, 256 b + 256) of every column into part[b, c]; then part's rows are
+// summed in order into out[c].
+constexpr uint32_t kColsumRows = 256;
+__global__ void k_colsum_part(const bf16* __restrict__ src, uint32_t R, uint32_t C, uint32_t lds,
+                              float* __restrict__ part) {
+  const uint32_t c = threadIdx.x, r0 = blockIdx.x * kColsumRows;
+  if (c >= C) return;
+  float s = 0.f;
+  const uint32_t r1 = min(R, r0 + kColsumRows);
+#pragma unroll 8
+  for (uint32_t r = r0; r < r1; ++r) s += __bfloat162float(src[(size_t)r * lds + c]);
+  part[(size_t)blockIdx.x * C + c] = s;
+}
+__global__ void k_colsum_final(const float* __restrict__ part, uint32_t nparts, uint32_t C, float* __restrict__ out) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
   float s = 0.f;
-  for (uint32_t r = 0; r < R; ++r) s += __bfloat162float(src[(size_t)r * lds + c]);
+  for (uint32_t p = 0; p < nparts; ++p) s += part[(size_t)p * C + c];
   out[c] = s;
 }
 
@@ -410,7 +423,7 @@ struct qpe_mlp {
   // activations
   DevBuf X0, pre1, pre2, pre3, H1, H2, H3, Y, dY, dZ1, dZ2, dZ3;
   DevBuf X0T, H1T, H2T, H3T, dYT, dZ1T, dZ2T, dZ3T;
-  DevBuf bla, bph, bw, loss, err, step;
+  DevBuf bla, bph, bw, loss, err, step, colpart;
   // training set
   DevBuf dbits, dla, dph, dw;
   uint64_t nsamples = 0;
@@ -453,6 +466,7 @@ static void mlp_alloc(qpe_mlp* m) {
   m->X0T.alloc(K0 * Bp * b2);
   for (DevBuf* p : {&m->H1T, &m->H2T, &m->H3T, &m->dZ1T, &m->dZ2T, &m->dZ3T}) p->alloc(H * Bp * b2);
   m->dYT.alloc(128 * Bp * b2);  // 128 rows for the M = 128 tile; rows past 63 stay zero
+  m->colpart.alloc(((Bp + 255) / 256) * H * 4);
   m->bla.alloc(Bp * 4);
   m->bph.alloc(Bp * 4);
   m->bw.alloc(Bp * 4);
@@ -518,10 +532,10 @@ static void forward(qpe_mlp* m, cudaStream_t s) {
 
 // Loss, backward and the gradients of every parameter into m->grads (W4 rows
 // 0..15 and the bias sums copied into their blocks).
-static void backward(qpe_mlp* m, uint32_t count, cudaStream_t s) {
+static void backward(qpe_mlp* m, uint32_t count, cudaStream_t s, float* loss) {
   const uint32_t B = m->Bp;
   k_loss<<<(B + 255) / 256, 256, 0, s>>>(m->Y.as<float>(), m->bla.as<float>(), m->bph.as<float>(),
-                                         m->bw.as<float>(), count, B, m->dY.as<bf16>(), m->loss.as<float>());
+                                         m->bw.as<float>(), count, B, m->dY.as<bf16>(), loss);
   QPE_CK(cudaGetLastError());
   for (const Gemm& g : m->bwd) QPE_CK(launch_gemm(g, s));
   const dim3 tb(32, 8);
@@ -540,10 +554,15 @@ static void backward(qpe_mlp* m, uint32_t count, cudaStream_t s) {
   for (const Gemm& g : m->wgrad) QPE_CK(launch_gemm(g, s));
   float* G = m->grads.as<float>();
   QPE_CK(cudaMemcpyAsync(G + qpe_mlp::oW4, G + qpe_mlp::nparams, 16 * 256 * 4, cudaMemcpyDeviceToDevice, s));
-  k_colsum<<<1, 256, 0, s>>>(m->dZ1.as<bf16>(), B, 256, 256, G + qpe_mlp::ob1);
-  k_colsum<<<1, 256, 0, s>>>(m->dZ2.as<bf16>(), B, 256, 256, G + qpe_mlp::ob2);
-  k_colsum<<<1, 256, 0, s>>>(m->dZ3.as<bf16>(), B, 256, 256, G + qpe_mlp::ob3);
-  k_colsum<<<1, 32, 0, s>>>(m->dY.as<bf16>(), B, 16, 64, G + qpe_mlp::ob4);
+  const uint32_t nparts = (B + kColsumRows - 1) / kColsumRows;
+  auto colsum = [&](const DevBuf& src, uint32_t C, uint32_t lds, float* out) {
+    k_colsum_part<<<nparts, 256, 0, s>>>(src.as<bf16>(), B, C, lds, m->colpart.as<float>());
+    k_colsum_final<<<1, 256, 0, s>>>(m->colpart.as<float>(), nparts, C, out);
+  };
+  colsum(m->dZ1, 256, 256, G + qpe_mlp::ob1);
+  colsum(m->dZ2, 256, 256, G + qpe_mlp::ob2);
+  colsum(m->dZ3, 256, 256, G + qpe_mlp::ob3);
+  colsum(m->dY, 16, 64, G + qpe_mlp::ob4);
   QPE_CK(cudaGetLastError());
 }
 
@@ -690,22 +709,24 @@ int qpe_mlp_train(qpe_mlp* m, uint32_t steps, float lr, uint64_t seed, float* lo
     if (!m->nsamples) throw Error(QPE_ERR_INVALID, "no training data (qpe_mlp_set_data)");
     use_ctx(m->ctx);
     cudaStream_t s = m->ctx->stream;
+    DevBuf hist;  // per-step losses, copied back once
+    hist.alloc((size_t)std::max(steps, 1u) * 4);
+    QPE_CK(cudaMemsetAsync(hist.p, 0, hist.bytes, s));
     for (uint32_t t = 0; t < steps; ++t) {
       ++m->adam_t;
       const float c1 = 1.0f / (1.0f - std::pow(0.9f, (float)m->adam_t));
       const float c2 = 1.0f / (1.0f - std::pow(0.999f, (float)m->adam_t));
-      QPE_CK(cudaMemsetAsync(m->loss.p, 0, 4, s));
       k_gather_batch<<<m->Bp, 64, 0, s>>>(m->dbits.as<uint64_t>(), m->dla.as<float>(), m->dph.as<float>(),
                                            m->dw.as<float>(), m->nsamples, m->Bp, m->Bp, m->n_bits, 1, seed,
                                            m->step.as<uint64_t>(), m->X0.as<bf16>(), m->bla.as<float>(),
                                            m->bph.as<float>(), m->bw.as<float>());
       QPE_CK(cudaGetLastError());
       forward(m, s);
-      backward(m, m->Bp, s);
+      backward(m, m->Bp, s, hist.as<float>() + t);
       adam(m, lr, s, c1, c2);
       k_add_u64<<<1, 1, 0, s>>>(m->step.as<uint64_t>(), 1);
-      if (losses) QPE_CK(cudaMemcpyAsync(losses + t, m->loss.p, 4, cudaMemcpyDeviceToHost, s));
     }
+    if (losses) QPE_CK(cudaMemcpyAsync(losses, hist.p, (size_t)steps * 4, cudaMemcpyDeviceToHost, s));
     QPE_CK(cudaStreamSynchronize(s));
     check_err(m);
   });
@@ -760,7 +781,7 @@ int qpe_mlp_gradients(qpe_mlp* m, const uint64_t* bits, const float* log_abs, co
                                          m->bla.as<float>(), m->bph.as<float>(), m->bw.as<float>());
     QPE_CK(cudaGetLastError());
     forward(m, s);
-    backward(m, count, s);
+    backward(m, count, s, m->loss.as<float>());
     QPE_CK(cudaMemcpyAsync(grads, m->grads.p, qpe_mlp::nparams * 4, cudaMemcpyDeviceToHost, s));
     if (loss) QPE_CK(cudaMemcpyAsync(loss, m->loss.p, 4, cudaMemcpyDeviceToHost, s));
     QPE_CK(cudaStreamSynchronize(s));

@@ -57,7 +57,15 @@ __device__ __forceinline__ void warp_copy(uint32_t n, uint32_t lane, Ok ok, Src 
   }
 }
 
-template <typename R, class A>
+size_t resident_meta_bytes(uint32_t nops, uint32_t pool_words, uint32_t npasses, uint32_t Ca, uint32_t Cb) {
+  return (size_t)nops * sizeof(DevOp) + (size_t)((pool_words + 3u) & ~3u) * 4 + (size_t)npasses * sizeof(Pass) +
+         (size_t)(Ca + Cb) * 4;
+}
+
+// MS: the program's metadata (term descriptors, index pool, passes, line strings)
+// is copied into every CTA's shared memory at the start, so that the term loop
+// reads it at shared-memory latency instead of through L1 / L2.
+template <typename R, class A, bool MS>
 __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __restrict__ insts, uint32_t stage_elems) {
   using C2 = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -84,6 +92,38 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
     return cta_ptr(blk, r, K) + (size_t)(a - r * Rk) * Cb + b;
   };
 
+  const DevOp* ops = I.ops;
+  const uint32_t* pool = I.pool;
+  const Pass* passes = I.passes;
+  const uint32_t* strA = I.strA;
+  const uint32_t* strB = I.strB;
+  if constexpr (MS) {
+    const size_t head = ((size_t)Rk * Cb + (size_t)wpc * stage_elems) * sizeof(C2);
+    unsigned char* meta = smem_raw + ((head + 15) & ~(size_t)15);
+    DevOp* ops_s = reinterpret_cast<DevOp*>(meta);
+    uint32_t* pool_s = reinterpret_cast<uint32_t*>(meta + (size_t)I.nops * sizeof(DevOp));
+    Pass* passes_s = reinterpret_cast<Pass*>(pool_s + ((I.pool_words + 3u) & ~3u));
+    uint32_t* strA_s = reinterpret_cast<uint32_t*>(passes_s + I.npasses);
+    uint32_t* strB_s = strA_s + Ca;
+    const uint4* osrc = reinterpret_cast<const uint4*>(I.ops);
+    for (uint32_t i = threadIdx.x; i < I.nops * 2; i += blockDim.x) reinterpret_cast<uint4*>(ops_s)[i] = osrc[i];
+    for (uint32_t i = threadIdx.x; i < I.pool_words; i += blockDim.x) pool_s[i] = I.pool[i];
+    const uint32_t* psrc = reinterpret_cast<const uint32_t*>(I.passes);
+    for (uint32_t i = threadIdx.x; i < I.npasses * (uint32_t)(sizeof(Pass) / 4); i += blockDim.x)
+      reinterpret_cast<uint32_t*>(passes_s)[i] = psrc[i];
+    for (uint32_t i = threadIdx.x; i < Ca; i += blockDim.x) strA_s[i] = I.strA[i];
+    for (uint32_t i = threadIdx.x; i < Cb; i += blockDim.x) strB_s[i] = I.strB[i];
+    ops = ops_s;
+    pool = pool_s;
+    passes = passes_s;
+    strA = strA_s;
+    strB = strB_s;
+  }
+  constexpr bool G = !MS;
+  // distributed-shared-memory loads in flight per lane in the tile gathers
+  // (fewer for complex128, whose 16-byte elements cost registers)
+  constexpr int kGatherDepth = sizeof(R) == 8 ? 2 : 4;
+
   // Block first - 1 (block first when evolving in place) into shared memory.
   {
     const C2* src = gstate + (uint64_t)(I.in_place ? I.first : I.first - 1) * ld + (uint64_t)row0 * Cb;
@@ -99,7 +139,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
     const bool rev = I.order == 2 && (sw & 1);
     for (uint32_t pj = 0; pj < I.npasses; ++pj) {
       const uint32_t pi = rev ? I.npasses - 1 - pj : pj;
-      const Pass P = I.passes[pi];
+      const Pass P = passes[pi];
       if (P.type == PASS_ROW) {
         // Rows owned by this CTA, Wr rows per warp tile, in place.
         const uint32_t W = I.Wr, logW = __ffs(W) - 1, w = lane & (W - 1);
@@ -108,9 +148,9 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
         for (uint32_t tile = warp; tile < ntiles; tile += wpc) {
           const uint32_t r = row0 + (tile << logW) + w;
           const bool active = r < row1;
-          const uint32_t lstr = active ? __ldg(I.strA + r) : 0u;
+          const uint32_t lstr = active ? ldm<G>(strA + r) : 0u;
           C2* line = blk + (size_t)(active ? r - row0 : 0) * Cb;
-          run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, Cb, jl, jstep, active, lstr,
+          run_line_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Cb, jl, jstep, active, lstr,
                              [&](uint32_t e) -> C2& { return line[e]; });
         }
       } else if (P.type == PASS_COL) {
@@ -121,21 +161,21 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
         for (uint32_t tile = gw; tile < ntiles; tile += nw) {
           const uint32_t b0 = tile << logW, c = b0 + w;
           const bool active = c < Cb;
-          const uint32_t lstr = active ? __ldg(I.strB + c) : 0u;
+          const uint32_t lstr = active ? ldm<G>(strB + c) : 0u;
           if (K == 1) {
             C2* col = blk + (active ? c : 0);
-            run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, Ca, jl, jstep, active, lstr,
+            run_line_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, jl, jstep, active, lstr,
                                [&](uint32_t e) -> C2& { return col[(size_t)e * Cb]; });
           } else {
             const uint32_t nl = min(W, Cb - b0);
             auto ok = [&](uint32_t i) { return (i & (W - 1)) < nl; };
             auto remote = [&](uint32_t i) { return at(i >> logW, b0 + (i & (W - 1))); };
             auto local = [&](uint32_t i) { return stage + i; };
-            warp_copy<C2, 4>(Ca << logW, lane, ok, remote, local);
+            warp_copy<C2, kGatherDepth>(Ca << logW, lane, ok, remote, local);
             __syncwarp();
-            run_line_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, Ca, jl, jstep, active, lstr,
+            run_line_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, jl, jstep, active, lstr,
                                [&](uint32_t e) -> C2& { return stage[(e << logW) + w]; });
-            warp_copy<C2, 4>(Ca << logW, lane, ok, local, remote);
+            warp_copy<C2, kGatherDepth>(Ca << logW, lane, ok, local, remote);
             __syncwarp();
           }
         }
@@ -144,14 +184,14 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
         const uint32_t jl = lane >> logW, jstep = 32 >> logW;
         const uint32_t ntiles = (P.mixcount + W - 1) >> logW;
         const uint32_t gw = warp * K + rank, nw = K * wpc;  // tile t on CTA t % K
-        const uint2* __restrict__ mt = reinterpret_cast<const uint2*>(I.pool + P.mixtab);
+        const uint2* __restrict__ mt = reinterpret_cast<const uint2*>(pool + P.mixtab);
         for (uint32_t tile = gw; tile < ntiles; tile += nw) {
           const uint32_t t0 = tile << logW, t = t0 + w;
           const bool active = t < P.mixcount;
-          const uint2 bp = active ? __ldg(mt + t) : make_uint2(0u, 0u);
+          const uint2 bp = active ? ldm<G>(mt + t) : make_uint2(0u, 0u);
           const uint32_t b01 = bp.x & 0x7fffffffu, b10 = bp.y, parb = bp.x >> 31;
           if (K == 1) {
-            run_mix_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, jl, jstep, active, parb,
+            run_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, jl, jstep, active, parb,
                               [&](uint32_t a) -> C2& { return blk[(size_t)a * Cb + b01]; },
                               [&](uint32_t a) -> C2& { return blk[(size_t)a * Cb + b10]; });
           } else {
@@ -160,17 +200,17 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
             // lane's column of element i: column-pair (i >> 1) & (W - 1), side i & 1;
             // with 32 a multiple of 2W it is the same for every i of the lane.
             const uint32_t mysel = lane & (2 * W - 1);
-            const uint2 myq = ((mysel >> 1) < nl) ? __ldg(mt + t0 + (mysel >> 1)) : make_uint2(0u, 0u);
+            const uint2 myq = ((mysel >> 1) < nl) ? ldm<G>(mt + t0 + (mysel >> 1)) : make_uint2(0u, 0u);
             const uint32_t mycol = (mysel & 1) ? myq.y : (myq.x & 0x7fffffffu);
             auto ok = [&](uint32_t) { return (mysel >> 1) < nl; };
             auto remote = [&](uint32_t i) { return at(i >> (logW + 1), mycol); };
             auto local = [&](uint32_t i) { return stage + i; };
-            warp_copy<C2, 4>(n2, lane, ok, remote, local);
+            warp_copy<C2, kGatherDepth>(n2, lane, ok, remote, local);
             __syncwarp();
-            run_mix_ops<R, A>(I.ops, I.coef, I.pool, P.op0, P.op1, rev, jl, jstep, active, parb,
+            run_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, jl, jstep, active, parb,
                               [&](uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w]; },
                               [&](uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w + 1]; });
-            warp_copy<C2, 4>(n2, lane, ok, local, remote);
+            warp_copy<C2, kGatherDepth>(n2, lane, ok, local, remote);
             __syncwarp();
           }
         }
@@ -185,7 +225,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
   }
 }
 
-template <typename R, class A>
+template <typename R, class A, bool MS>
 static cudaError_t launch_res(const ResidentLaunch& rl, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(rl.ninst * rl.cluster);
@@ -199,55 +239,48 @@ static cudaError_t launch_res(const ResidentLaunch& rl, cudaStream_t s) {
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaError_t e = cudaFuncSetAttribute(k_resident<R, A>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_resident<R, A, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)rl.smem_bytes);
   if (e) return e;
   if (rl.cluster > 8) {
-    e = cudaFuncSetAttribute(k_resident<R, A>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    e = cudaFuncSetAttribute(k_resident<R, A, MS>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e) return e;
   }
-  e = cudaLaunchKernelEx(&cfg, k_resident<R, A>, rl.insts, rl.stage_elems);
+  e = cudaLaunchKernelEx(&cfg, k_resident<R, A, MS>, rl.insts, rl.stage_elems);
   return e;
 }
 
-cudaError_t launch_resident(const ResidentLaunch& rl, int dtype, int exact, cudaStream_t s) {
+template <bool MS>
+static cudaError_t launch_resident_ms(const ResidentLaunch& rl, int dtype, int exact, cudaStream_t s) {
   if (dtype == QPE_C128) {
-    if (exact) return launch_res<double, ExactD>(rl, s);
-    return launch_res<double, Fast<double>>(rl, s);
+    if (exact) return launch_res<double, ExactD, MS>(rl, s);
+    return launch_res<double, Fast<double>, MS>(rl, s);
   }
-  return launch_res<float, Fast<float>>(rl, s);
+  return launch_res<float, Fast<float>, MS>(rl, s);
+}
+
+cudaError_t launch_resident(const ResidentLaunch& rl, int dtype, int exact, cudaStream_t s) {
+  return rl.meta_smem ? launch_resident_ms<true>(rl, dtype, exact, s) : launch_resident_ms<false>(rl, dtype, exact, s);
+}
+
+template <bool MS>
+static cudaError_t carveout_ms(int dtype, int exact, int percent) {
+  if (dtype == QPE_C128) {
+    if (exact)
+      return cudaFuncSetAttribute(k_resident<double, ExactD, MS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  percent);
+    return cudaFuncSetAttribute(k_resident<double, Fast<double>, MS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                percent);
+  }
+  return cudaFuncSetAttribute(k_resident<float, Fast<float>, MS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                              percent);
 }
 
 cudaError_t set_resident_carveout(int dtype, int exact, int percent) {
-  if (dtype == QPE_C128) {
-    if (exact)
-      return cudaFuncSetAttribute(k_resident<double, ExactD>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
-    return cudaFuncSetAttribute(k_resident<double, Fast<double>>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                percent);
-  }
-  return cudaFuncSetAttribute(k_resident<float, Fast<float>>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+  cudaError_t e = carveout_ms<false>(dtype, exact, percent);
+  if (e) return e;
+  return carveout_ms<true>(dtype, exact, percent);
 }
 
-cudaError_t resident_max_cluster(int dtype, uint32_t cluster, uint32_t warps, size_t smem, int* max_clusters) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(cluster);
-  cfg.blockDim = dim3(32 * warps);
-  cfg.dynamicSmemBytes = smem;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = cluster;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  if (dtype == QPE_C128) {
-    cudaFuncSetAttribute(k_resident<double, ExactD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (cluster > 8) cudaFuncSetAttribute(k_resident<double, ExactD>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    return cudaOccupancyMaxActiveClusters(max_clusters, k_resident<double, ExactD>, &cfg);
-  }
-  cudaFuncSetAttribute(k_resident<float, Fast<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cluster > 8) cudaFuncSetAttribute(k_resident<float, Fast<float>>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  return cudaOccupancyMaxActiveClusters(max_clusters, k_resident<float, Fast<float>>, &cfg);
-}
 
 }  // namespace qpe

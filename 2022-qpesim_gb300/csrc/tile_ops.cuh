@@ -44,6 +44,15 @@ struct Fast {
   static __device__ __forceinline__ R sub(R a, R b) { return a - b; }
 };
 
+// Metadata load: through the read-only data cache when the program's tables and
+// term descriptors are in global memory (G), a plain load when a kernel has
+// staged them in shared memory.
+template <bool G, class T>
+__device__ __forceinline__ T ldm(const T* p) {
+  if constexpr (G) return __ldg(p);
+  else return *p;
+}
+
 template <typename R>
 struct Coef4 {
   R e0r, e0i, e1r, e1i, o0r, o0i, o1r, o1i;
@@ -60,12 +69,12 @@ struct OpR {
 // icoef, when given, replaces the inline (c0, c1) of op o with icoef[o]: the
 // instances of a batch share one program's structure and keep their own
 // coefficients.
-template <typename R>
+template <typename R, bool G = true>
 __device__ __forceinline__ OpR<R> load_op(const DevOp* __restrict__ ops, const double* __restrict__ coef, uint32_t o,
                                           const double2* __restrict__ icoef = nullptr) {
   OpR<R> r;
   const uint4* src = reinterpret_cast<const uint4*>(ops + o);
-  const uint4 a = __ldg(src), b = __ldg(src + 1);
+  const uint4 a = ldm<G>(src), b = ldm<G>(src + 1);
   r.d.tab = a.x;
   r.d.count = a.y;
   r.d.kind = (uint8_t)(a.z & 0xff);
@@ -155,7 +164,7 @@ __device__ __forceinline__ bool cond_ok(uint32_t line_str, const DevOp& op) {
 // coefficients and this lane's first table entry are loaded while the current
 // term computes, so the chain of dependent terms pays shared-memory latency
 // rather than the latency of the metadata loads.
-template <typename R, class A, class Elem>
+template <typename R, class A, bool G = true, class Elem>
 __device__ __forceinline__ void run_line_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
                                              const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1, bool rev,
                                              uint32_t L, uint32_t jl, uint32_t jstep, bool active, uint32_t lstr,
@@ -164,16 +173,16 @@ __device__ __forceinline__ void run_line_ops(const DevOp* __restrict__ ops, cons
   if (n == 0) return;
   auto at = [&](uint32_t i) { return rev ? op1 - 1 - i : op0 + i; };
   auto first_of = [&](const DevOp& d) -> uint2 {
-    return (d.kind == OPK_PAIR && jl < d.count) ? __ldg(reinterpret_cast<const uint2*>(pool + d.tab) + jl)
+    return (d.kind == OPK_PAIR && jl < d.count) ? ldm<G>(reinterpret_cast<const uint2*>(pool + d.tab) + jl)
                                                 : make_uint2(0u, 0u);
   };
-  OpR<R> op = load_op<R>(ops, coef, at(0), icoef);
+  OpR<R> op = load_op<R, G>(ops, coef, at(0), icoef);
   uint2 first = first_of(op.d);
   for (uint32_t i = 0; i < n; ++i) {
     OpR<R> opn = op;
     uint2 firstn = make_uint2(0u, 0u);
     if (i + 1 < n) {
-      opn = load_op<R>(ops, coef, at(i + 1), icoef);
+      opn = load_op<R, G>(ops, coef, at(i + 1), icoef);
       firstn = first_of(opn.d);
     }
     const DevOp& d = op.d;
@@ -183,12 +192,12 @@ __device__ __forceinline__ void run_line_ops(const DevOp* __restrict__ ops, cons
         uint2 x = first;
         for (uint32_t j = jl; j < d.count; j += jstep) {
           const uint32_t jn = j + jstep;
-          const uint2 xn = jn < d.count ? __ldg(t + jn) : make_uint2(0u, 0u);
+          const uint2 xn = jn < d.count ? ldm<G>(t + jn) : make_uint2(0u, 0u);
           pair_update<A>(elem(x.x & 0x7fffffffu), elem(x.y), op.k, x.x >> 31);
           x = xn;
         }
       } else if (d.kind == OPK_DIAG_LIST) {
-        for (uint32_t j = jl; j < d.count; j += jstep) diag_update<A>(elem(__ldg(pool + d.tab + j)), op.k);
+        for (uint32_t j = jl; j < d.count; j += jstep) diag_update<A>(elem(ldm<G>(pool + d.tab + j)), op.k);
       } else {
         for (uint32_t e = jl; e < L; e += jstep) diag_update<A>(elem(e), op.k);
       }
@@ -203,7 +212,7 @@ __device__ __forceinline__ void run_line_ops(const DevOp* __restrict__ ops, cons
 // (reverse order when `rev`): entry (a01 | par, a10) pairs left(a01) with
 // right(a10), parity adding the beta pair's parity parb
 // (cpp/time_evolution_over_terms.hpp:774). Pipelined as run_line_ops.
-template <typename R, class A, class Left, class Right>
+template <typename R, class A, bool G = true, class Left, class Right>
 __device__ __forceinline__ void run_mix_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
                                             const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1, bool rev,
                                             uint32_t jl, uint32_t jstep, bool active, uint32_t parb, Left left,
@@ -212,15 +221,15 @@ __device__ __forceinline__ void run_mix_ops(const DevOp* __restrict__ ops, const
   if (n == 0) return;
   auto at = [&](uint32_t i) { return rev ? op1 - 1 - i : op0 + i; };
   auto first_of = [&](const DevOp& d) -> uint2 {
-    return jl < d.count ? __ldg(reinterpret_cast<const uint2*>(pool + d.tab) + jl) : make_uint2(0u, 0u);
+    return jl < d.count ? ldm<G>(reinterpret_cast<const uint2*>(pool + d.tab) + jl) : make_uint2(0u, 0u);
   };
-  OpR<R> op = load_op<R>(ops, coef, at(0), icoef);
+  OpR<R> op = load_op<R, G>(ops, coef, at(0), icoef);
   uint2 first = first_of(op.d);
   for (uint32_t i = 0; i < n; ++i) {
     OpR<R> opn = op;
     uint2 firstn = make_uint2(0u, 0u);
     if (i + 1 < n) {
-      opn = load_op<R>(ops, coef, at(i + 1), icoef);
+      opn = load_op<R, G>(ops, coef, at(i + 1), icoef);
       firstn = first_of(opn.d);
     }
     if (active) {
@@ -228,7 +237,7 @@ __device__ __forceinline__ void run_mix_ops(const DevOp* __restrict__ ops, const
       uint2 x = first;
       for (uint32_t j = jl; j < op.d.count; j += jstep) {
         const uint32_t jn = j + jstep;
-        const uint2 xn = jn < op.d.count ? __ldg(t + jn) : make_uint2(0u, 0u);
+        const uint2 xn = jn < op.d.count ? ldm<G>(t + jn) : make_uint2(0u, 0u);
         pair_update<A>(left(x.x & 0x7fffffffu), right(x.y), op.k, (x.x >> 31) ^ parb);
         x = xn;
       }

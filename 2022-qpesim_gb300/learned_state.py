@@ -122,3 +122,112 @@ class AmplitudeMLP:
         f = C.c_double()
         N.check(self._lib.qpe_mlp_tensor_flops_per_step(self._h, C.byref(f)))
         return f.value
+
+
+# ---- the learned-state pipeline ---------------------------------------------------
+
+def colex_rank(bv: int) -> int:
+    """OffsetComputer::rank (cpp/offset_computer.hpp:16-27): sum_i C(pos_i, i + 1)."""
+    r, order, pos = 0, 1, 0
+    while bv:
+        if bv & 1:
+            r += math.comb(pos, order)
+            order += 1
+        bv >>= 1
+        pos += 1
+    return r
+
+
+def colex_strings(nbits: int, weight: int) -> np.ndarray:
+    """The weight-`weight` strings of nbits bits in rank order."""
+    from itertools import combinations
+    strs = [sum(1 << i for i in c) for c in combinations(range(nbits), weight)]
+    strs.sort(key=colex_rank)
+    return np.array(strs, np.uint64)
+
+
+def register_strings(M: int, na: int, nb: int) -> np.ndarray:
+    """Occupation string of every amplitude of a block, in register order (alpha
+    rank major, beta rank minor); alpha orbitals are bits 0..M-1, beta M..2M-1
+    (the HalfUp convention of cpp/types.hpp:50-55)."""
+    a = colex_strings(M, na)
+    b = colex_strings(M, nb)
+    return (a[:, None] | (b[None, :] << np.uint64(M))).ravel()
+
+
+def state_targets(psi: np.ndarray, floor: float = 1e-6):
+    """Training targets of one state: log|a| (floored), phase with the largest
+    amplitude made real and positive, and weights |a|^2 * dim + 0.05 (mean ~1)."""
+    psi = np.asarray(psi, np.complex128)
+    psi = psi / np.linalg.norm(psi)
+    j = int(np.argmax(np.abs(psi)))
+    psi = psi * np.exp(-1j * np.angle(psi[j]))
+    a = np.abs(psi)
+    return (np.log(np.maximum(a, floor)).astype(np.float32), np.angle(psi).astype(np.float32),
+            (a * a * len(psi) + 0.05).astype(np.float32))
+
+
+def proposed_state(model: AmplitudeMLP, strings: np.ndarray) -> np.ndarray:
+    """The model's state over `strings`, normalised to 1."""
+    out = model.forward(strings).astype(np.float64)
+    amp = np.exp(out[:, 0] - out[:, 0].max()) * np.exp(1j * out[:, 1])
+    return amp / np.linalg.norm(amp)
+
+
+def ground_bin(probs: np.ndarray, t_power: float, rel: float = 0.02) -> int:
+    """The lowest-energy local maximum of the histogram holding at least `rel`
+    of the largest bin (the Fejer side lobes of one peak decay monotonically, so
+    they are not local maxima)."""
+    from .readout import phase_to_energy
+    n = len(probs)
+    thr = rel * float(probs.max())
+    cand = [j for j in range(n) if probs[j] >= thr and probs[j] >= probs[(j - 1) % n] and probs[j] >= probs[(j + 1) % n]]
+    return int(min(cand, key=lambda j: phase_to_energy(j / n, t_power)))
+
+
+def window_mass(probs: np.ndarray, j0: int, half: int = 1) -> float:
+    n = len(probs)
+    return float(sum(probs[(j0 + d) % n] for d in range(-half, half + 1)))
+
+
+def subbin_energy(freq: np.ndarray, j0: int, n: int, t_power: float) -> float:
+    """Energy from the histogram (or shot frequencies) around bin j0: peak bin
+    refined by the amplitude ratio of its larger neighbour."""
+    from .readout import phase_to_energy
+    a0 = math.sqrt(max(freq[j0 % n], 0.0))
+    left, right = math.sqrt(max(freq[(j0 - 1) % n], 0.0)), math.sqrt(max(freq[(j0 + 1) % n], 0.0))
+    if right >= left:
+        d = right / (a0 + right) if a0 + right > 0 else 0.0
+    else:
+        d = -left / (a0 + left) if a0 + left > 0 else 0.0
+    return phase_to_energy(((j0 + d) / n) % 1.0, t_power)
+
+
+def shots_to_precision(probs: np.ndarray, j0: int, t_power: float, e_target: float, tol: float = 1e-3,
+                       trials: int = 16, seed: int = 0, max_shots: int = 1 << 22):
+    """Smallest number of QPE shots (on a doubling grid) after which the sub-bin
+    estimate from the shots landing in the ground window j0 +- 1 is within `tol`
+    of e_target in at least 90% of `trials` simulated experiments. None when the
+    noiseless estimate itself misses `tol` or max_shots is not enough."""
+    n = len(probs)
+    p = np.clip(np.asarray(probs, np.float64), 0, None)
+    p = p / p.sum()
+    if abs(subbin_energy(p, j0, n, t_power) - e_target) > tol:
+        return None
+    rng = np.random.default_rng(seed)
+    shots = 16
+    while shots <= max_shots:
+        ok = 0
+        for _ in range(trials):
+            f = rng.multinomial(shots, p).astype(np.float64)
+            if f[[(j0 - 1) % n, j0 % n, (j0 + 1) % n]].sum() == 0:
+                continue
+            # the estimate uses the peak of the observed window
+            w = [(j0 + d) % n for d in (-1, 0, 1)]
+            jm = w[int(np.argmax(f[w]))]
+            if abs(subbin_energy(f, jm, n, t_power) - e_target) <= tol:
+                ok += 1
+        if ok >= 0.9 * trials:
+            return shots
+        shots *= 2
+    return None
