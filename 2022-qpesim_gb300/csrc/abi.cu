@@ -204,8 +204,10 @@ static uint32_t choose_lines(uint64_t lines, uint64_t nwarps, uint64_t entries) 
 }
 
 // Geometry of the resident kernel for cluster size K; false if it does not fit.
+// group: tiles processed by four-warp groups (k_resident_group), one stage per
+// group; otherwise by single warps (k_resident), one stage per warp.
 static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K, ResidentLaunch& rl,
-                          ResidentInstance& ri) {
+                          ResidentInstance& ri, bool group = false) {
   const HostProgram& hp = pr->hp;
   const size_t esz = st->esz;
   const uint64_t Ca = hp.Ca, Cb = hp.Cb;
@@ -219,26 +221,28 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
   // block (and warp stages) alone.
   for (int with_meta = 1; with_meta >= 0; --with_meta)
   for (uint32_t wpc = 16; wpc >= 4; wpc /= 2) {
+    // units that own tiles: warps, or groups of four warps (32 quad slots each)
+    const uint32_t units = group ? wpc / 4 : wpc;
     ri = ResidentInstance{};
     ri.Ca = (uint32_t)Ca;
     ri.Cb = (uint32_t)Cb;
     ri.rows_per_cta = (uint32_t)Rk;
     // typical table lengths: CA over alpha (COL / MIX), CA over beta (ROW)
     const uint64_t ea = binom((int)hp.M - 2, (int)hp.na - 1), eb = binom((int)hp.M - 2, (int)hp.nb - 1);
-    ri.Wr = choose_lines(Rk, wpc, eb ? eb : 1);
-    ri.Wc = choose_lines(Cb, (uint64_t)K * wpc, ea ? ea : 1);
-    // at most 16 column pairs per tile: a lane's gather column is then fixed
-    ri.Wm = std::min<uint32_t>(16u, choose_lines(mixcount ? mixcount : 1, (uint64_t)K * wpc, ea ? ea : 1));
+    ri.Wr = choose_lines(Rk, units, eb ? eb : 1);
+    ri.Wc = choose_lines(Cb, (uint64_t)K * units, ea ? ea : 1);
+    // at most 16 column pairs per tile: a thread's gather column is then fixed
+    ri.Wm = std::min<uint32_t>(16u, choose_lines(mixcount ? mixcount : 1, (uint64_t)K * units, ea ? ea : 1));
     uint64_t stage = 0;
     if (K > 1) {
       while (true) {
         stage = std::max<uint64_t>(Ca * ri.Wc, 2 * Ca * ri.Wm);
-        if (Rk * Cb * esz + wpc * stage * esz <= st->ctx->smem_optin || (ri.Wc == 1 && ri.Wm == 1)) break;
+        if (Rk * Cb * esz + units * stage * esz <= st->ctx->smem_optin || (ri.Wc == 1 && ri.Wm == 1)) break;
         if (ri.Wc > 1) ri.Wc /= 2;
         if (ri.Wm > 1 && 2 * Ca * ri.Wm > Ca * ri.Wc) ri.Wm /= 2;
       }
     }
-    const size_t head = (size_t)(Rk * Cb * esz + wpc * stage * esz);
+    const size_t head = (size_t)(Rk * Cb * esz + units * stage * esz);
     const size_t smem = with_meta ? ((head + 15) & ~(size_t)15) + meta : head;
     if (smem <= st->ctx->smem_optin) {
       rl = ResidentLaunch{};
@@ -247,6 +251,7 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
       rl.warps_per_cta = wpc;
       rl.stage_elems = (uint32_t)stage;
       rl.meta_smem = (uint32_t)with_meta;
+      rl.group = group ? 1u : 0u;
       rl.smem_bytes = smem < 1024 ? 1024 : smem;
       return true;
     }
@@ -255,10 +260,11 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
 }
 
 static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint32_t first, uint32_t last,
-                         bool exact, bool in_place = false) {
+                         bool exact, bool in_place = false, bool group = false) {
   ResidentLaunch rl;
   ResidentInstance ri{};
-  if (!plan_resident(pr, st, K, rl, ri)) throw Error(QPE_ERR_UNSUPPORTED, "block does not fit the cluster's shared memory");
+  if (!plan_resident(pr, st, K, rl, ri, group))
+    throw Error(QPE_ERR_UNSUPPORTED, "block does not fit the cluster's shared memory");
   ri.state = st->data.p;
   ri.pool = pr->pool.as<uint32_t>();
   ri.ops = pr->ops.as<DevOp>();
@@ -298,10 +304,11 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     K = 1;
     return;
   }
-  if (strategy == QPE_STRATEGY_CLUSTER) {
+  if (strategy == QPE_STRATEGY_CLUSTER || strategy == QPE_STRATEGY_GROUP) {
+    const bool grp = strategy == QPE_STRATEGY_GROUP;
     if (K == 0) {
-      for (uint32_t c = 2; c <= 16 && !K; c *= 2)
-        if (plan_resident(pr, st, c, rl, ri)) K = c;
+      for (uint32_t c = grp ? 1 : 2; c <= 16 && !K; c *= 2)
+        if (plan_resident(pr, st, c, rl, ri, grp)) K = c;
       if (!K) throw Error(QPE_ERR_UNSUPPORTED, "block does not fit a cluster of 16");
     }
     return;
@@ -324,8 +331,10 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     ~Restore() { cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, s); cudaStreamSynchronize(s); }
   } restore{block1, saved.p, st->ld * st->esz, st->ctx->stream};
   std::vector<std::pair<uint32_t, uint32_t>> cands;
-  for (uint32_t c = 1; c <= 16; c *= 2)
+  for (uint32_t c = 1; c <= 16; c *= 2) {
     if (plan_resident(pr, st, c, rl, ri)) cands.push_back({c == 1 ? QPE_STRATEGY_RESIDENT : QPE_STRATEGY_CLUSTER, c});
+    if (plan_resident(pr, st, c, rl, ri, true)) cands.push_back({QPE_STRATEGY_GROUP, c});
+  }
   cands.push_back({QPE_STRATEGY_TILED, 0});
   if (cands.size() == 1) {
     strategy = QPE_STRATEGY_TILED;
@@ -338,7 +347,7 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
       float ms = 0;
       auto run = [&]() {
         if (c.first == QPE_STRATEGY_TILED) evolve_tiled(st, pr, 1, 2, exact);
-        else run_resident(st, pr, c.second, 1, 2, exact);
+        else run_resident(st, pr, c.second, 1, 2, exact, false, c.first == QPE_STRATEGY_GROUP);
       };
       try {
         run();  // warm-up of this configuration
@@ -401,7 +410,7 @@ static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* 
   if (strategy == QPE_STRATEGY_TILED) {
     evolve_tiled(st, pr, first, last, exact, in_place);
   } else {
-    run_resident(st, pr, K, first, last, exact, in_place);
+    run_resident(st, pr, K, first, last, exact, in_place, strategy == QPE_STRATEGY_GROUP);
     QPE_CK(cudaStreamSynchronize(st->ctx->stream));
   }
 }
@@ -863,7 +872,7 @@ int qpe_evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts
   return guard([&] {
     check_state(st);
     if (!pr) throw Error(QPE_ERR_INVALID, "null program");
-    if (opts && opts->strategy > QPE_STRATEGY_TILED) throw Error(QPE_ERR_INVALID, "unknown strategy");
+    if (opts && opts->strategy > QPE_STRATEGY_GROUP) throw Error(QPE_ERR_INVALID, "unknown strategy");
     if (opts && opts->cluster_size && (opts->cluster_size > 16 || (opts->cluster_size & (opts->cluster_size - 1))))
       throw Error(QPE_ERR_INVALID, "cluster_size must be a power of two <= 16");
     if (opts && (opts->flags & ~(QPE_EVOLVE_FP64_CONTRACT | QPE_EVOLVE_IN_PLACE)))

@@ -46,7 +46,6 @@ __global__ void k_pass(PassLaunch pl) {
   else if (PT == PASS_ROW) ntiles = Ca;
   else ntiles = pl.pass.mixcount;
   const uint32_t nmem = pl.nmem ? pl.nmem : 1u;
-
   for (uint32_t gt = blockIdx.x * wpc + warp; gt < ntiles * nmem; gt += gridDim.x * wpc) {
     const uint32_t mem = gt / ntiles, tile = gt - mem * ntiles;
     C2* __restrict__ blk = reinterpret_cast<C2*>(pl.works ? pl.works[mem] : pl.work);

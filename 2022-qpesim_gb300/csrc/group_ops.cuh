@@ -1,0 +1,107 @@
+// group_ops.cuh - term application by a group of warps with every amplitude
+// update split over four lanes.
+//
+// On GB300 a warp's FP64 instruction occupies its SM sub-partition's FP64 unit
+// for many cycles, so a term applied by one warp costs (FP64 instructions per
+// lane) x that issue time however many other warps are idle. Here a tile is
+// processed by a group of warps (one per sub-partition) and each pair update of
+// updateStateVector (cpp/time_evolution_over_terms.hpp:565-589) is done by a
+// quad of lanes: lane q of the quad computes one real component of the result
+// (l'.re, l'.im, r'.re, r'.im). Every component is the same expression, in the
+// same operation order, as in pair_update (tile_ops.cuh), written as
+//   out = x1*c1 + x2*c2                 (m00 real, m01 imaginary: 3 FP64 ops)
+//   out = (x1*c1 + x2*c2) + (x3*c3 + x4*c4)   (general 2 x 2 matrix)
+// with a subtraction written as the addition of the exactly negated product,
+// so the result is bit-identical to the reference's complex arithmetic. Lanes
+// pick their operands by q, so the quad runs one instruction stream.
+//
+// Within one term the pairs are disjoint; the quad reads both amplitudes of its
+// pair before any lane writes (a warp barrier between the two), and a group
+// barrier separates consecutive terms.
+#ifndef QPE_GROUP_OPS_CUH_
+#define QPE_GROUP_OPS_CUH_
+
+#include "tile_ops.cuh"
+
+namespace qpe {
+
+// One term after another on a tile of W lines. left(w, e) / right(w, e) are the
+// amplitudes a pair entry (e01, e10) of line w pairs up (the same accessor for
+// a COL or ROW line; the b01 and b10 columns of column pair w in a MIX tile);
+// diagonal terms use left. lstr(w) is line w's occupation string (for the
+// terms' conditions), nvalid the number of real lines (< W at the block's
+// edge), parb(w) the beta-pair parity of MIX column pair w (0 otherwise; MIX
+// terms carry no conditions). gt is the thread's index in the group, gthreads
+// the group size, gbar() the group barrier.
+template <typename R, class A, bool G, class Left, class Right, class Lstr, class Parb, class Bar>
+__device__ __forceinline__ void group_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
+                                          const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1, bool rev,
+                                          uint32_t L, uint32_t logW, uint32_t nvalid, bool mix, uint32_t gt,
+                                          uint32_t gthreads, Left left, Right right, Lstr lstr, Parb parb, Bar gbar) {
+  using C2 = typename Cx<R>::T;
+  const uint32_t n = op1 - op0;
+  const uint32_t q = gt & 3u, slot = gt >> 2, nslots = gthreads >> 2;
+  const uint32_t W = 1u << logW;
+  for (uint32_t i = 0; i < n; ++i) {
+    const OpR<R> op = load_op<R, G>(ops, coef, rev ? op1 - 1 - i : op0 + i);
+    const DevOp& d = op.d;
+    const Coef4<R>& k = op.k;
+    const uint32_t per_line = d.kind == OPK_DIAG_ALL ? L : d.count;
+    const uint32_t nitems = per_line << logW;
+    for (uint32_t base = 0; base < nitems; base += nslots) {
+      const uint32_t item = base + slot;
+      const uint32_t w = item & (W - 1), j = item >> logW;
+      bool act = item < nitems && w < nvalid;
+      if (act && !mix && d.ncond) act = cond_ok(lstr(w), d);
+      R out = (R)0;
+      C2* dst = nullptr;
+      if (act) {
+        if (d.kind == OPK_PAIR) {
+          const uint2 x = ldm<G>(reinterpret_cast<const uint2*>(pool + d.tab) + j);
+          C2& lref = left(w, x.x & 0x7fffffffu);
+          C2& rref = right(w, x.y);
+          const C2 vl = lref, vr = rref;
+          const uint32_t par = (x.x >> 31) ^ parb(w);
+          const R m0r = par ? k.o0r : k.e0r, m0i = par ? k.o0i : k.e0i;
+          const R m1r = par ? k.o1r : k.e1r, m1i = par ? k.o1i : k.e1i;
+          if (k.reduced) {
+            // l'.re = lx c - ry t, l'.im = ly c + rx t, r'.re = rx c - ly t, r'.im = lx t + ry c
+            const R x1 = q == 0 ? vl.x : q == 1 ? vl.y : q == 2 ? vr.x : vl.x;
+            const R c1 = q == 3 ? m1i : m0r;
+            const R x2 = q == 0 ? vr.y : q == 1 ? vr.x : q == 2 ? vl.y : vr.y;
+            const R c2 = q == 3 ? m0r : ((q & 1) ? m1i : -m1i);
+            out = A::add(A::mul(x1, c1), A::mul(x2, c2));
+          } else {
+            // l' = l m00 + r m01, r' = l m01 + r m00, every complex product (ac - bd, ad + bc)
+            const R ma_r = q < 2 ? m0r : m1r, ma_i = q < 2 ? m0i : m1i;  // multiplies l
+            const R mb_r = q < 2 ? m1r : m0r, mb_i = q < 2 ? m1i : m0i;  // multiplies r
+            const bool im = q & 1;
+            const R c1 = im ? ma_i : ma_r, c2 = im ? ma_r : -ma_i;
+            const R c3 = im ? mb_i : mb_r, c4 = im ? mb_r : -mb_i;
+            out = A::add(A::add(A::mul(vl.x, c1), A::mul(vl.y, c2)), A::add(A::mul(vr.x, c3), A::mul(vr.y, c4)));
+          }
+          C2& t = (q < 2) ? lref : rref;
+          dst = &t;
+        } else if (q < 2) {
+          const uint32_t e = d.kind == OPK_DIAG_LIST ? ldm<G>(pool + d.tab + j) : j;
+          C2& vref = left(w, e);
+          const C2 v = vref;
+          // (vx c.r - vy c.i, vx c.i + vy c.r)
+          const R c1 = q ? k.e0i : k.e0r, c2 = q ? k.e0r : -k.e0i;
+          out = A::add(A::mul(v.x, c1), A::mul(v.y, c2));
+          dst = &vref;
+        }
+      }
+      __syncwarp();
+      if (dst) {
+        R* comp = reinterpret_cast<R*>(dst);
+        comp[q & 1] = out;
+      }
+    }
+    gbar();
+  }
+}
+
+}  // namespace qpe
+
+#endif  // QPE_GROUP_OPS_CUH_

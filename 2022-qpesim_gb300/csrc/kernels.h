@@ -87,6 +87,8 @@ struct ResidentLaunch {
   uint32_t cluster;               // CTAs per instance (1 = one CTA)
   uint32_t warps_per_cta;
   uint32_t stage_elems;           // per-warp stage (cluster > 1)
+  uint32_t group;                 // 1: four-warp tile groups with quad-split updates
+                                  //    (k_resident_group); stage_elems is then per group
   uint32_t meta_smem;             // 1: term descriptors, index pool, passes and line
                                   //    strings are staged in every CTA's shared memory
   size_t smem_bytes;

@@ -23,6 +23,7 @@
 #include <cudaTypedefs.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -46,6 +47,8 @@ struct GemmArgs {
   float* pre_out;        // EPI_BIAS_GELU: pre-activation, FP32, stride ldo
   const float* pre_in;   // EPI_DGELU: the forward pre-activation, FP32, stride ldo
   int* err;              // set when a wait runs out
+  uint32_t ksplit;       // EPI_F32: CTAs along K (grid z); slice z writes out + z * split_stride
+  size_t split_stride;
 };
 
 constexpr uint32_t kStages = 4;
@@ -78,7 +81,10 @@ __global__ void __launch_bounds__(128, 1)
   uint32_t* slot = reinterpret_cast<uint32_t*>(basep + kStages * kStage + (2 * kStages + 1) * 8);
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t m0 = blockIdx.y * 128, n0 = blockIdx.x * BN;
-  const uint32_t nk = g.K / 64;
+  // k-blocks of this CTA's K slice (all of K unless split)
+  const uint32_t nk_all = g.K / 64, ks = g.ksplit ? g.ksplit : 1u;
+  const uint32_t kb0 = (uint32_t)((uint64_t)nk_all * blockIdx.z / ks);
+  const uint32_t nk = (uint32_t)((uint64_t)nk_all * (blockIdx.z + 1) / ks) - kb0;
 
   if (threadIdx.x == 0) {
     for (uint32_t s = 0; s < kStages; ++s) {
@@ -99,8 +105,8 @@ __global__ void __launch_bounds__(128, 1)
     auto issue = [&](uint32_t kb, uint32_t s) {
       const uint32_t a = base + s * kStage;
       umma::mbar_expect_tx(full(s), kStage);
-      umma::tma_load_2d(a, &ta, (int32_t)(kb * 64), (int32_t)m0, full(s));
-      umma::tma_load_2d(a + kABytes, &tb, (int32_t)(kb * 64), (int32_t)n0, full(s));
+      umma::tma_load_2d(a, &ta, (int32_t)((kb0 + kb) * 64), (int32_t)m0, full(s));
+      umma::tma_load_2d(a + kABytes, &tb, (int32_t)((kb0 + kb) * 64), (int32_t)n0, full(s));
     };
     const uint32_t idesc = umma::idesc_bf16(128, BN);
     uint32_t issued = 0, kb = 0;
@@ -148,7 +154,7 @@ __global__ void __launch_bounds__(128, 1)
     const uint32_t col = n0 + c;
     const size_t off = (size_t)row * g.ldo + col;
     if (EPI == EPI_F32 || EPI == EPI_BIAS_F32) {
-      float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(g.out) + off);
+      float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(g.out) + off + blockIdx.z * g.split_stride);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         float4 x = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
@@ -195,6 +201,19 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // ---- small kernels of the training step ---------------------------------------
+
+// out[r, c] = sum over slices z (in order) of part[z][r, c]: the fixed-order
+// reduction of a split-K product (rows x cols, row stride ld in both).
+__global__ void k_reduce_split(const float* __restrict__ part, uint32_t ks, size_t stride, uint32_t rows,
+                               uint32_t cols, uint32_t ld, float* __restrict__ out, uint32_t ldo) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)rows * cols) return;
+  const size_t r = i / cols, c = i - r * cols;
+  float s = 0.f;
+  for (uint32_t z = 0; z < ks; ++z) s += part[z * stride + r * ld + c];
+  out[r * ldo + c] = s;
+}
+
 
 // dst[C, R] = src[R, C]^T (BF16), 32 x 32 tiles through shared memory.
 __global__ void k_transpose(const bf16* __restrict__ src, bf16* __restrict__ dst, uint32_t R, uint32_t C,
@@ -366,6 +385,8 @@ struct Gemm {
   GemmArgs g;
   int epi;
   uint32_t bn;
+  float* final_out = nullptr;  // split-K: the reduced product's destination
+  uint32_t final_ldo = 0;
 };
 
 template <int EPI, uint32_t BN>
@@ -373,7 +394,14 @@ static cudaError_t launch_gemm_t(const Gemm& G, cudaStream_t s) {
   constexpr size_t smem = gemm_smem_bytes<BN>();
   cudaError_t e = cudaFuncSetAttribute(k_gemm<EPI, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e) return e;
-  k_gemm<EPI, BN><<<dim3(G.g.N / BN, G.g.M / 128), 128, smem, s>>>(G.ta, G.tb, G.g);
+  const uint32_t ks = G.g.ksplit ? G.g.ksplit : 1u;
+  k_gemm<EPI, BN><<<dim3(G.g.N / BN, G.g.M / 128, ks), 128, smem, s>>>(G.ta, G.tb, G.g);
+  e = cudaGetLastError();
+  if (e || ks == 1 || !G.final_out) return e;
+  const size_t n = (size_t)G.g.M * G.g.N;
+  k_reduce_split<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(reinterpret_cast<const float*>(G.g.out), ks,
+                                                             G.g.split_stride, G.g.M, G.g.N, G.g.ldo, G.final_out,
+                                                             G.final_ldo);
   return cudaGetLastError();
 }
 
@@ -400,9 +428,29 @@ static Gemm make_gemm(int epi, uint32_t bn, const void* A, uint32_t lda, const v
   Gemm G;
   G.ta = make_map(A, M, K, lda, 128);
   G.tb = make_map(B, N, K, ldb, bn);
-  G.g = GemmArgs{M, N, K, bias, out, ldo, pre_out, pre_in, err};
+  G.g = GemmArgs{M, N, K, bias, out, ldo, pre_out, pre_in, err, 1u, 0};
   G.epi = epi;
   G.bn = bn;
+  return G;
+}
+
+// A plain FP32 product split along K over enough CTAs to fill the GPU: the
+// slices write partial tiles into `scratch` (ksplit x M x N) and a fixed-order
+// reduction writes the result to out.
+static Gemm make_gemm_splitk(uint32_t bn, const void* A, uint32_t lda, const void* B, uint32_t ldb, uint32_t M,
+                             uint32_t N, uint32_t K, float* out, uint32_t ldo, float* scratch, size_t scratch_elems,
+                             uint32_t num_sms, int* err) {
+  const uint32_t tiles = (M / 128) * (N / bn), nk = K / 64;
+  uint32_t ks = std::max(1u, std::min(nk, (num_sms + tiles - 1) / tiles));
+  while (ks > 1 && (size_t)ks * M * N > scratch_elems) --ks;
+  Gemm G = make_gemm(EPI_F32, bn, A, lda, B, ldb, M, N, K, ks > 1 ? scratch : out, ks > 1 ? N : ldo, nullptr,
+                     nullptr, nullptr, err);
+  G.g.ksplit = ks;
+  G.g.split_stride = (size_t)M * N;
+  if (ks > 1) {
+    G.final_out = out;
+    G.final_ldo = ldo;
+  }
   return G;
 }
 
@@ -423,7 +471,7 @@ struct qpe_mlp {
   // activations
   DevBuf X0, pre1, pre2, pre3, H1, H2, H3, Y, dY, dZ1, dZ2, dZ3;
   DevBuf X0T, H1T, H2T, H3T, dYT, dZ1T, dZ2T, dZ3T;
-  DevBuf bla, bph, bw, loss, err, step, colpart;
+  DevBuf bla, bph, bw, loss, err, step, colpart, splitk;
   // training set
   DevBuf dbits, dla, dph, dw;
   uint64_t nsamples = 0;
@@ -467,6 +515,8 @@ static void mlp_alloc(qpe_mlp* m) {
   for (DevBuf* p : {&m->H1T, &m->H2T, &m->H3T, &m->dZ1T, &m->dZ2T, &m->dZ3T}) p->alloc(H * Bp * b2);
   m->dYT.alloc(128 * Bp * b2);  // 128 rows for the M = 128 tile; rows past 63 stay zero
   m->colpart.alloc(((Bp + 255) / 256) * H * 4);
+  const size_t splitk_elems = (size_t)64 * 256 * 256;  // up to 64 K slices of a 256 x 256 gradient
+  m->splitk.alloc(splitk_elems * 4);
   m->bla.alloc(Bp * 4);
   m->bph.alloc(Bp * 4);
   m->bw.alloc(Bp * 4);
@@ -498,15 +548,16 @@ static void mlp_alloc(qpe_mlp* m) {
                 m->pre1.as<float>(), err)};
   // dW4 is [128, 256] over the padded dY^T, stored past the parameter blocks;
   // its rows 0..15 are copied into the W4 block.
-  m->wgrad = {
-      make_gemm(EPI_F32, 64, m->dZ1T.p, B, m->X0T.p, B, 256, 64, B, G + qpe_mlp::oW1, 64, nullptr, nullptr, nullptr,
-                err),
-      make_gemm(EPI_F32, 256, m->dZ2T.p, B, m->H1T.p, B, 256, 256, B, G + qpe_mlp::oW2, 256, nullptr, nullptr,
-                nullptr, err),
-      make_gemm(EPI_F32, 256, m->dZ3T.p, B, m->H2T.p, B, 256, 256, B, G + qpe_mlp::oW3, 256, nullptr, nullptr,
-                nullptr, err),
-      make_gemm(EPI_F32, 256, m->dYT.p, B, m->H3T.p, B, 128, 256, B, G + qpe_mlp::nparams, 256, nullptr, nullptr,
-                nullptr, err)};
+  const uint32_t sms = (uint32_t)m->ctx->num_sms;
+  float* sk = m->splitk.as<float>();
+  m->wgrad = {make_gemm_splitk(64, m->dZ1T.p, B, m->X0T.p, B, 256, 64, B, G + qpe_mlp::oW1, 64, sk, splitk_elems,
+                               sms, err),
+              make_gemm_splitk(256, m->dZ2T.p, B, m->H1T.p, B, 256, 256, B, G + qpe_mlp::oW2, 256, sk, splitk_elems,
+                               sms, err),
+              make_gemm_splitk(256, m->dZ3T.p, B, m->H2T.p, B, 256, 256, B, G + qpe_mlp::oW3, 256, sk, splitk_elems,
+                               sms, err),
+              make_gemm_splitk(256, m->dYT.p, B, m->H3T.p, B, 128, 256, B, G + qpe_mlp::nparams, 256, sk,
+                               splitk_elems, sms, err)};
   const double Bd = (double)B;
   m->tensor_flops_per_step = 2.0 * Bd * (256.0 * 64 + 2 * 256.0 * 256 + 16.0 * 256)      // forward
                              + 2.0 * Bd * (256.0 * 64 + 2 * 256.0 * 256)                  // backward data
@@ -810,7 +861,11 @@ int qpe_gemm_bf16(qpe_context* ctx, uint32_t M, uint32_t N, uint32_t K, const ui
     QPE_CK(cudaMemset(e.p, 0, 16));
     QPE_CK(cudaMemcpy(dA.p, A, (size_t)M * K * 2, cudaMemcpyHostToDevice));
     QPE_CK(cudaMemcpy(dB.p, B, (size_t)N * K * 2, cudaMemcpyHostToDevice));
-    Gemm G = make_gemm(EPI_F32, tile_n, dA.p, K, dB.p, K, M, N, K, dD.p, N, nullptr, nullptr, nullptr, e.as<int>());
+    DevBuf scratch;
+    const size_t se = (size_t)M * N * 16;
+    scratch.alloc(se * 4);
+    Gemm G = make_gemm_splitk(tile_n, dA.p, K, dB.p, K, M, N, K, dD.as<float>(), N, scratch.as<float>(), se,
+                              (uint32_t)ctx->num_sms, e.as<int>());
     QPE_CK(launch_gemm(G, ctx->stream));
     QPE_CK(cudaStreamSynchronize(ctx->stream));
     int err = 0;

@@ -25,6 +25,7 @@
 #include <stdint.h>
 
 #include "kernels.h"
+#include "group_ops.cuh"
 #include "tile_ops.cuh"
 
 namespace cg = cooperative_groups;
@@ -52,6 +53,25 @@ __device__ __forceinline__ void warp_copy(uint32_t n, uint32_t lane, Ok ok, Src 
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const uint32_t i = base + 32 * u;
+      if (i < n && ok(i)) *dst(i) = v[u];
+    }
+  }
+}
+
+// warp_copy for a group of gthreads threads (thread gt): elements gt, gt +
+// gthreads, ...
+template <typename V, int U, class Ok, class Src, class Dst>
+__device__ __forceinline__ void group_copy(uint32_t n, uint32_t gt, uint32_t gthreads, Ok ok, Src src, Dst dst) {
+  for (uint32_t base = gt; base < n; base += gthreads * U) {
+    V v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t i = base + gthreads * u;
+      if (i < n && ok(i)) v[u] = *src(i);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t i = base + gthreads * u;
       if (i < n && ok(i)) *dst(i) = v[u];
     }
   }
@@ -225,6 +245,165 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
   }
 }
 
+// The same evolution with tiles processed by groups of four warps (one per SM
+// sub-partition) and every update split over a quad of lanes (group_ops.cuh):
+// a term's FP64 work is spread over the four FP64 units of the SM instead of
+// one. Tiles (rows, columns or column pairs) go to the cluster's groups
+// round-robin; stage_elems is per group.
+constexpr uint32_t kGroupWarps = 4;
+
+template <typename R, class A, bool MS>
+__global__ void __launch_bounds__(512) k_resident_group(const ResidentInstance* __restrict__ insts,
+                                                        uint32_t stage_elems) {
+  using C2 = typename Cx<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t K = cl.num_blocks();
+  const uint32_t rank = cl.block_rank();
+  const ResidentInstance I = insts[blockIdx.x / K];
+  const uint32_t wpc = blockDim.x >> 5;
+  const uint32_t gthreads = 32 * kGroupWarps, ngrp = wpc / kGroupWarps;
+  const uint32_t grp = threadIdx.x / gthreads, gt = threadIdx.x - grp * gthreads;
+  const uint32_t Ca = I.Ca, Cb = I.Cb, Rk = I.rows_per_cta;
+  const uint32_t row0 = min(rank * Rk, Ca), row1 = min(row0 + Rk, Ca);
+  C2* blk = reinterpret_cast<C2*>(smem_raw);
+  C2* stage = blk + (size_t)Rk * Cb + (size_t)grp * stage_elems;
+  C2* __restrict__ gstate = reinterpret_cast<C2*>(I.state);
+  const uint64_t ld = (uint64_t)Ca * Cb;
+  const uint32_t nown = (row1 - row0) * Cb;
+
+  auto barrier = [&]() {
+    if (K == 1) __syncthreads();
+    else cl.sync();
+  };
+  auto gbar = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(gthreads) : "memory"); };
+  auto at = [&](uint32_t a, uint32_t b) -> C2* {
+    const uint32_t r = a / Rk;
+    return cta_ptr(blk, r, K) + (size_t)(a - r * Rk) * Cb + b;
+  };
+
+  const DevOp* ops = I.ops;
+  const uint32_t* pool = I.pool;
+  const Pass* passes = I.passes;
+  const uint32_t* strA = I.strA;
+  const uint32_t* strB = I.strB;
+  if constexpr (MS) {
+    const size_t head = ((size_t)Rk * Cb + (size_t)ngrp * stage_elems) * sizeof(C2);
+    unsigned char* meta = smem_raw + ((head + 15) & ~(size_t)15);
+    DevOp* ops_s = reinterpret_cast<DevOp*>(meta);
+    uint32_t* pool_s = reinterpret_cast<uint32_t*>(meta + (size_t)I.nops * sizeof(DevOp));
+    Pass* passes_s = reinterpret_cast<Pass*>(pool_s + ((I.pool_words + 3u) & ~3u));
+    uint32_t* strA_s = reinterpret_cast<uint32_t*>(passes_s + I.npasses);
+    uint32_t* strB_s = strA_s + Ca;
+    const uint4* osrc = reinterpret_cast<const uint4*>(I.ops);
+    for (uint32_t i = threadIdx.x; i < I.nops * 2; i += blockDim.x) reinterpret_cast<uint4*>(ops_s)[i] = osrc[i];
+    for (uint32_t i = threadIdx.x; i < I.pool_words; i += blockDim.x) pool_s[i] = I.pool[i];
+    const uint32_t* psrc = reinterpret_cast<const uint32_t*>(I.passes);
+    for (uint32_t i = threadIdx.x; i < I.npasses * (uint32_t)(sizeof(Pass) / 4); i += blockDim.x)
+      reinterpret_cast<uint32_t*>(passes_s)[i] = psrc[i];
+    for (uint32_t i = threadIdx.x; i < Ca; i += blockDim.x) strA_s[i] = I.strA[i];
+    for (uint32_t i = threadIdx.x; i < Cb; i += blockDim.x) strB_s[i] = I.strB[i];
+    ops = ops_s;
+    pool = pool_s;
+    passes = passes_s;
+    strA = strA_s;
+    strB = strB_s;
+  }
+  constexpr bool G = !MS;
+  constexpr int kDepth = sizeof(R) == 8 ? 2 : 4;
+  auto no_parity = [](uint32_t) { return 0u; };
+
+  {
+    const C2* src = gstate + (uint64_t)(I.in_place ? I.first : I.first - 1) * ld + (uint64_t)row0 * Cb;
+    for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) blk[i] = src[i];
+  }
+  barrier();
+
+  const uint32_t nsweeps = I.steps * I.order;
+  for (uint32_t k = I.first; k < I.last; ++k) {
+    for (uint32_t sw = 0; sw < nsweeps; ++sw) {
+      const bool rev = I.order == 2 && (sw & 1);
+      for (uint32_t pj = 0; pj < I.npasses; ++pj) {
+        const uint32_t pi = rev ? I.npasses - 1 - pj : pj;
+        const Pass P = passes[pi];
+        if (P.type == PASS_ROW) {
+          // this CTA's rows, Wr per group tile, in place
+          const uint32_t W = I.Wr, logW = __ffs(W) - 1;
+          const uint32_t ntiles = (row1 - row0 + W - 1) >> logW;
+          for (uint32_t tile = grp; tile < ntiles; tile += ngrp) {
+            const uint32_t r0 = row0 + (tile << logW), nv = min(W, row1 - r0);
+            auto line = [&](uint32_t w, uint32_t e) -> C2& { return blk[(size_t)(r0 - row0 + w) * Cb + e]; };
+            group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Cb, logW, nv, false, gt, gthreads, line, line,
+                               [&](uint32_t w) { return ldm<G>(strA + r0 + w); }, no_parity, gbar);
+          }
+        } else if (P.type == PASS_COL) {
+          const uint32_t W = I.Wc, logW = __ffs(W) - 1;
+          const uint32_t ntiles = (Cb + W - 1) >> logW;
+          for (uint32_t tile = grp * K + rank; tile < ntiles; tile += K * ngrp) {
+            const uint32_t b0 = tile << logW, nv = min(W, Cb - b0);
+            auto lstr = [&](uint32_t w) { return ldm<G>(strB + b0 + w); };
+            if (K == 1) {
+              auto line = [&](uint32_t w, uint32_t e) -> C2& { return blk[(size_t)e * Cb + b0 + w]; };
+              group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, logW, nv, false, gt, gthreads, line, line,
+                                 lstr, no_parity, gbar);
+            } else {
+              auto ok = [&](uint32_t i) { return (i & (W - 1)) < nv; };
+              auto remote = [&](uint32_t i) { return at(i >> logW, b0 + (i & (W - 1))); };
+              auto local = [&](uint32_t i) { return stage + i; };
+              group_copy<C2, kDepth>(Ca << logW, gt, gthreads, ok, remote, local);
+              gbar();
+              auto line = [&](uint32_t w, uint32_t e) -> C2& { return stage[(e << logW) + w]; };
+              group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, logW, nv, false, gt, gthreads, line, line,
+                                 lstr, no_parity, gbar);
+              group_copy<C2, kDepth>(Ca << logW, gt, gthreads, ok, local, remote);
+              gbar();
+            }
+          }
+        } else {  // PASS_MIX: Wm column pairs per group tile
+          const uint32_t W = I.Wm, logW = __ffs(W) - 1;
+          const uint32_t ntiles = (P.mixcount + W - 1) >> logW;
+          const uint2* __restrict__ mt = reinterpret_cast<const uint2*>(pool + P.mixtab);
+          for (uint32_t tile = grp * K + rank; tile < ntiles; tile += K * ngrp) {
+            const uint32_t t0 = tile << logW, nv = min(W, P.mixcount - t0);
+            auto pair_of = [&](uint32_t w) { return ldm<G>(mt + t0 + w); };
+            auto parb = [&](uint32_t w) { return pair_of(w).x >> 31; };
+            if (K == 1) {
+              auto left = [&](uint32_t w, uint32_t a) -> C2& {
+                return blk[(size_t)a * Cb + (pair_of(w).x & 0x7fffffffu)];
+              };
+              auto right = [&](uint32_t w, uint32_t a) -> C2& { return blk[(size_t)a * Cb + pair_of(w).y]; };
+              group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, logW, nv, true, gt, gthreads, left, right,
+                                 no_parity, parb, gbar);
+            } else {
+              // element i: row i >> (logW + 1), column pair (i >> 1) & (W - 1), side i & 1; with
+              // gthreads a multiple of 2W a thread's column is the same for all its elements
+              const uint32_t mysel = gt & (2 * W - 1);
+              const uint2 myq = ((mysel >> 1) < nv) ? pair_of(mysel >> 1) : make_uint2(0u, 0u);
+              const uint32_t mycol = (mysel & 1) ? myq.y : (myq.x & 0x7fffffffu);
+              auto ok = [&](uint32_t) { return (mysel >> 1) < nv; };
+              auto remote = [&](uint32_t i) { return at(i >> (logW + 1), mycol); };
+              auto local = [&](uint32_t i) { return stage + i; };
+              const uint32_t n2 = Ca << (logW + 1);
+              group_copy<C2, kDepth>(n2, gt, gthreads, ok, remote, local);
+              gbar();
+              auto left = [&](uint32_t w, uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w]; };
+              auto right = [&](uint32_t w, uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w + 1]; };
+              group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, logW, nv, true, gt, gthreads, left, right,
+                                 no_parity, parb, gbar);
+              group_copy<C2, kDepth>(n2, gt, gthreads, ok, local, remote);
+              gbar();
+            }
+          }
+        }
+        barrier();
+      }
+    }
+    C2* dst = gstate + (uint64_t)(I.in_place ? I.first : k) * ld + (uint64_t)row0 * Cb;
+    for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) dst[i] = blk[i];
+    barrier();
+  }
+}
+
 template <typename R, class A, bool MS>
 static cudaError_t launch_res(const ResidentLaunch& rl, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
@@ -239,14 +418,14 @@ static cudaError_t launch_res(const ResidentLaunch& rl, cudaStream_t s) {
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaError_t e = cudaFuncSetAttribute(k_resident<R, A, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)rl.smem_bytes);
+  auto kern = rl.group ? k_resident_group<R, A, MS> : k_resident<R, A, MS>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rl.smem_bytes);
   if (e) return e;
   if (rl.cluster > 8) {
-    e = cudaFuncSetAttribute(k_resident<R, A, MS>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e) return e;
   }
-  e = cudaLaunchKernelEx(&cfg, k_resident<R, A, MS>, rl.insts, rl.stage_elems);
+  e = cudaLaunchKernelEx(&cfg, kern, rl.insts, rl.stage_elems);
   return e;
 }
 
@@ -263,17 +442,20 @@ cudaError_t launch_resident(const ResidentLaunch& rl, int dtype, int exact, cuda
   return rl.meta_smem ? launch_resident_ms<true>(rl, dtype, exact, s) : launch_resident_ms<false>(rl, dtype, exact, s);
 }
 
+template <typename R, class A, bool MS>
+static cudaError_t carveout_t(int percent) {
+  cudaError_t e = cudaFuncSetAttribute(k_resident<R, A, MS>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+  if (e) return e;
+  return cudaFuncSetAttribute(k_resident_group<R, A, MS>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+}
+
 template <bool MS>
 static cudaError_t carveout_ms(int dtype, int exact, int percent) {
   if (dtype == QPE_C128) {
-    if (exact)
-      return cudaFuncSetAttribute(k_resident<double, ExactD, MS>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                  percent);
-    return cudaFuncSetAttribute(k_resident<double, Fast<double>, MS>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                percent);
+    if (exact) return carveout_t<double, ExactD, MS>(percent);
+    return carveout_t<double, Fast<double>, MS>(percent);
   }
-  return cudaFuncSetAttribute(k_resident<float, Fast<float>, MS>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                              percent);
+  return carveout_t<float, Fast<float>, MS>(percent);
 }
 
 cudaError_t set_resident_carveout(int dtype, int exact, int percent) {

@@ -142,7 +142,8 @@ class DeviceState:
                cluster_size: int = 0, fp64_contract: bool = False) -> None:
         """strategy: 0 auto (autotuned per program), 1 one CTA resident in shared
         memory, 2 a cluster of cluster_size CTAs (0: smallest that fits), 3
-        global-memory tile passes. fp64_contract allows FMAs in complex128
+        global-memory tile passes, 4 a cluster whose tiles are processed by
+        four-warp groups with every update split over four lanes. fp64_contract allows FMAs in complex128
         (within 1e-12 of the reference instead of bit-identical)."""
         opts = N.EvolveOpts(strategy, first_power, last_power, cluster_size,
                             N.QPE_EVOLVE_FP64_CONTRACT if fp64_contract else 0, 0)
@@ -165,7 +166,7 @@ class DeviceState:
         return p
 
     def last_strategy(self) -> tuple:
-        """(strategy, cluster size) of the last evolve: 1 resident, 2 cluster, 3 tiled."""
+        """(strategy, cluster size) of the last evolve: 1 resident, 2 cluster, 3 tiled, 4 grouped cluster."""
         s, k = C.c_uint32(), C.c_uint32()
         N.check(self._lib.qpe_state_last_strategy(self._h, C.byref(s), C.byref(k)))
         return s.value, k.value

@@ -285,9 +285,11 @@ def run_ours(args, w, rank, ws, local):
         kernel = "k_pass (evolution tile passes, one launch per pass)"
         launches = args.steps * (npow * (info["num_passes_per_power"] + 2) + 1 + 2 + 1)
     else:
-        kernel = f"k_resident (whole evolution in one launch, cluster of {kc} CTA(s))"
+        kernel = (f"{'k_resident_group' if strat == 4 else 'k_resident'} (whole evolution in one launch, "
+                  f"cluster of {kc} CTA(s))")
         launches = args.steps * (1 + 2)
-    strategy_name = {1: "resident (one CTA)", 2: f"cluster of {kc} CTAs", 3: "tiled passes"}.get(strat, "?")
+    strategy_name = {1: "resident (one CTA)", 2: f"cluster of {kc} CTAs", 3: "tiled passes",
+                     4: f"cluster of {kc} CTAs, four-warp tile groups"}.get(strat, "?")
     line = {
         "metric": "amplitude-term updates/s per Trotter step",
         "value": value,
@@ -705,7 +707,8 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--strategy", type=int, default=0, help="0 auto, 1 one-CTA resident, 2 cluster, 3 tiled")
+    ap.add_argument("--strategy", type=int, default=0,
+                    help="0 auto, 1 one-CTA resident, 2 cluster, 3 tiled, 4 cluster with four-warp groups")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per cluster for --strategy 2 (0: smallest)")
     ap.add_argument("--powers", type=int, default=0,
                     help="evolve only the first K controlled powers (profiling runs; not a workload's figure)")

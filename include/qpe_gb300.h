@@ -206,6 +206,8 @@ int qpe_state_zero(qpe_state* st);
 #define QPE_STRATEGY_RESIDENT 1 /* whole block in one CTA's shared memory */
 #define QPE_STRATEGY_CLUSTER 2  /* block spread over a thread-block cluster */
 #define QPE_STRATEGY_TILED 3    /* L2-resident block, shared-memory tile passes */
+#define QPE_STRATEGY_GROUP 4    /* as CLUSTER (cluster_size 1..16), tiles processed by four-warp
+                                   groups with every update split over four lanes */
 
 /* complex128 only: allow fused multiply-adds. Results then differ from the
  * reference's rounding by a few ulps per update (within 1e-12 of it) instead of
