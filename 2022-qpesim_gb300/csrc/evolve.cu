@@ -24,6 +24,17 @@
 
 namespace qpe {
 
+// One element from global to shared memory without passing through registers
+// (cp.async, 8 or 16 bytes; the caller commits and waits).
+template <typename C2>
+__device__ __forceinline__ void async_copy(C2* dst, const C2* src) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  if constexpr (sizeof(C2) == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+
 // One pass. PT selects the tile geometry (stage layout [entry][line]):
 //   PASS_COL: tile = W consecutive columns, stage[e * W + w] = block[e][b0 + w]
 //   PASS_ROW: tile = one row,               stage[e]         = block[a][e]
@@ -60,30 +71,19 @@ __global__ void k_pass(PassLaunch pl) {
       parb = x.x >> 31;
     }
     const uint32_t nl = (PT == PASS_COL) ? min(W, Cb - b0) : W;  // valid lines
-    // Element i of the stage <-> block offset g(i). Gathers keep kU loads in
-    // flight per lane before their shared-memory stores, so a tile pays the L2
-    // latency once per kU elements rather than once per element.
+    // Element i of the stage <-> block offset g(i). The gather is a stream of
+    // asynchronous global -> shared copies (cp.async), all in flight at once, so
+    // a tile pays the L2 latency once rather than once per element.
     auto goff = [&](uint32_t i) -> uint64_t {
       const uint32_t e = i >> logW, w = i & (W - 1);
       if (PT == PASS_COL) return (uint64_t)e * Cb + b0 + w;
       if (PT == PASS_ROW) return (uint64_t)row * Cb + e;
       return (uint64_t)e * Cb + (w ? b10 : b01);
     };
-    constexpr uint32_t kU = 8;
     const uint32_t nst = L * W;
-    for (uint32_t base = lane; base < nst; base += 32 * kU) {
-      C2 v[kU];
-#pragma unroll
-      for (uint32_t u = 0; u < kU; ++u) {
-        const uint32_t i = base + 32 * u;
-        if (i < nst && (i & (W - 1)) < nl) v[u] = blk[goff(i)];
-      }
-#pragma unroll
-      for (uint32_t u = 0; u < kU; ++u) {
-        const uint32_t i = base + 32 * u;
-        if (i < nst && (i & (W - 1)) < nl) st[i] = v[u];
-      }
-    }
+    for (uint32_t i = lane; i < nst; i += 32)
+      if ((i & (W - 1)) < nl) async_copy(st + i, blk + goff(i));
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
     __syncwarp();
     if (PT == PASS_MIX) {
       run_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, lane, 32, true, parb,
