@@ -69,15 +69,15 @@ __device__ __forceinline__ void group_ops(const DevOp* __restrict__ ops, const d
             const R x1 = q == 0 ? vl.x : q == 1 ? vl.y : q == 2 ? vr.x : vl.x;
             const R c1 = q == 3 ? m1i : m0r;
             const R x2 = q == 0 ? vr.y : q == 1 ? vr.x : q == 2 ? vl.y : vr.y;
-            const R c2 = q == 3 ? m0r : ((q & 1) ? m1i : -m1i);
+            const R c2 = q == 3 ? m0r : ((q & 1) ? m1i : neg(m1i));
             out = A::add(A::mul(x1, c1), A::mul(x2, c2));
           } else {
             // l' = l m00 + r m01, r' = l m01 + r m00, every complex product (ac - bd, ad + bc)
             const R ma_r = q < 2 ? m0r : m1r, ma_i = q < 2 ? m0i : m1i;  // multiplies l
             const R mb_r = q < 2 ? m1r : m0r, mb_i = q < 2 ? m1i : m0i;  // multiplies r
             const bool im = q & 1;
-            const R c1 = im ? ma_i : ma_r, c2 = im ? ma_r : -ma_i;
-            const R c3 = im ? mb_i : mb_r, c4 = im ? mb_r : -mb_i;
+            const R c1 = im ? ma_i : ma_r, c2 = im ? ma_r : neg(ma_i);
+            const R c3 = im ? mb_i : mb_r, c4 = im ? mb_r : neg(mb_i);
             out = A::add(A::add(A::mul(vl.x, c1), A::mul(vl.y, c2)), A::add(A::mul(vr.x, c3), A::mul(vr.y, c4)));
           }
           C2& t = (q < 2) ? lref : rref;
@@ -87,7 +87,7 @@ __device__ __forceinline__ void group_ops(const DevOp* __restrict__ ops, const d
           C2& vref = left(w, e);
           const C2 v = vref;
           // (vx c.r - vy c.i, vx c.i + vy c.r)
-          const R c1 = q ? k.e0i : k.e0r, c2 = q ? k.e0r : -k.e0i;
+          const R c1 = q ? k.e0i : k.e0r, c2 = q ? k.e0r : neg(k.e0i);
           out = A::add(A::mul(v.x, c1), A::mul(v.y, c2));
           dst = &vref;
         }

@@ -53,6 +53,14 @@ __device__ __forceinline__ T ldm(const T* p) {
   else return *p;
 }
 
+// Exact negation as a sign-bit flip on the integer pipe. On this GPU an FP64
+// instruction occupies a warp's FP64 unit for about 64 cycles, so a negation
+// written as FP64 arithmetic would cost as much as a product.
+__device__ __forceinline__ double neg(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+__device__ __forceinline__ float neg(float x) { return __int_as_float(__float_as_int(x) ^ (int)0x80000000u); }
+
 template <typename R>
 struct Coef4 {
   R e0r, e0i, e1r, e1i, o0r, o0i, o1r, o1i;
@@ -95,7 +103,7 @@ __device__ __forceinline__ OpR<R> load_op(const DevOp* __restrict__ ops, const d
     r.k.e0i = r.k.o0i = (R)0;
     r.k.e1r = r.k.o1r = (R)0;
     r.k.e1i = (R)r.d.c1;
-    r.k.o1i = -(R)r.d.c1;
+    r.k.o1i = neg((R)r.d.c1);
     r.k.reduced = r.d.kind == OPK_PAIR;
     if (r.d.kind != OPK_PAIR) r.k.e0i = (R)r.d.c1;
   } else {

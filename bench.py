@@ -135,15 +135,19 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def setup_dist():
+def setup_dist(backend="nccl"):
+    """Replicas: one process per GPU (RANK / LOCAL_RANK / WORLD_SIZE from the
+    launcher); the only collectives are the timing barrier and the max of the
+    per-rank times. backend "gloo" runs the same host logic on CPU."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if ws > 1:
         import torch
         import torch.distributed as dist
         local = int(os.environ.get("LOCAL_RANK", "0"))
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
         return rank, ws, local
     return 0, 1, 0
 
@@ -153,7 +157,8 @@ def reduce_max(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -326,7 +331,7 @@ def run_ours(args, w, rank, ws, local):
     }
     if args.powers:
         line["config"]["powers_evolved"] = npow
-    if w.get("check_c128"):
+    if w.get("check_c128") and not args.powers:
         line["precision_check"] = precision_check(q, w, seg, st, prog, block0, local)
     if rank == 0 and not args.no_cpu_baseline:
         rate, threads, sample = cpu_baseline(q, w, seg)
