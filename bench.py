@@ -331,6 +331,8 @@ def run_ours(args, w, rank, ws, local):
     }
     if args.powers:
         line["config"]["powers_evolved"] = npow
+    if args.precision:
+        line["config"]["precision_override"] = args.precision
     if w.get("check_c128") and not args.powers:
         line["precision_check"] = precision_check(q, w, seg, st, prog, block0, local)
     if rank == 0 and not args.no_cpu_baseline:
@@ -717,12 +719,16 @@ def main():
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per cluster for --strategy 2 (0: smallest)")
     ap.add_argument("--powers", type=int, default=0,
                     help="evolve only the first K controlled powers (profiling runs; not a workload's figure)")
+    ap.add_argument("--precision", type=int, default=0,
+                    help="override the ancilla count (profiling runs on a smaller register; not a workload's figure)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     rank, ws, local = setup_dist() if args.impl == "ours" else (int(os.environ.get("RANK", "0")),
                                                                  int(os.environ.get("WORLD_SIZE", "1")), 0)
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.precision:
+        w["P"] = args.precision
     if args.impl == "reference":
         line = run_reference(args, w, rank, ws)
     elif w.get("learned"):
