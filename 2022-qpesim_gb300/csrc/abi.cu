@@ -161,14 +161,22 @@ PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_opt
   uint32_t wpc = 4;
   while (wpc > 1 && stage * wpc > smem_optin) --wpc;
   uint64_t ntiles = pass.type == PASS_COL ? (hp.Cb + W - 1) / W : (pass.type == PASS_ROW ? hp.Ca : pass.mixcount);
-  if (esz == 16) {
+  // Long index tables (tens of entries per lane of a warp): one tile per CTA,
+  // whose threads split every term's entries, so a term's chain is short.
+  const uint64_t entries = binom((int)hp.M - 2, (int)(pass.type == PASS_ROW ? hp.nb : hp.na) - 1) *
+                           (pass.type == PASS_COL ? W : 1);
+  pl.cta_tile = entries >= 64 ? 1u : 0u;
+  if (pl.cta_tile) {
+    wpc = kCtaTileThreads / 32;
+  } else if (esz == 16) {
     // complex128 tiles are bound by the SM's FP64 issue rate: spread the tiles
     // over the SMs first, then stack warps.
     const uint64_t per_sm = (ntiles + pr->ctx->num_sms - 1) / pr->ctx->num_sms;
     wpc = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(wpc, per_sm));
   }
   pl.warps_per_cta = wpc;
-  uint64_t grid = (ntiles + wpc - 1) / wpc;
+  const uint32_t slots = pl.cta_tile ? 1u : wpc;
+  uint64_t grid = (ntiles + slots - 1) / slots;
   const uint64_t cap = (uint64_t)pr->ctx->num_sms * 8;
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
@@ -442,7 +450,7 @@ static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, u
         PassLaunch& pl = plans.back();
         pl.rev = rev ? 1u : 0u;
         pl.exact = exact ? 1u : 0u;
-        size_t sm = pass_stage_elems(pass, pl.Ca, pl.Cb, pl.W) * st->esz * pl.warps_per_cta;
+        size_t sm = pass_stage_elems(pass, pl.Ca, pl.Cb, pl.W) * st->esz * (pl.cta_tile ? 1 : pl.warps_per_cta);
         if (sm > max_smem) max_smem = sm;
       }
     }

@@ -89,12 +89,15 @@ void plan_class(qpe_batch* b, BatchClass& c) {
       PassLaunch pl = plan_pass_geometry(c.shape, b->esz, b->ctx->smem_optin, pass);
       if (pass.type == PASS_COL && c.W) pl.W = c.W;
       const size_t stage = pass_stage_elems(pass, pl.Ca, pl.Cb, pl.W) * b->esz;
-      uint32_t wpc = c.wpc;
-      while (wpc > 1 && stage * wpc > b->ctx->smem_optin) --wpc;
+      // wpc == 0 selects one tile per CTA (its threads split every term's entries)
+      pl.cta_tile = c.wpc == 0 ? 1u : 0u;
+      uint32_t wpc = c.wpc ? c.wpc : kCtaTileThreads / 32;
+      while (!pl.cta_tile && wpc > 1 && stage * wpc > b->ctx->smem_optin) --wpc;
       pl.warps_per_cta = wpc;
       const uint64_t ntiles = pass.type == PASS_COL ? (hp.Cb + pl.W - 1) / pl.W
                                                     : (pass.type == PASS_ROW ? hp.Ca : pass.mixcount);
-      uint64_t grid = (ntiles * c.members.size() + wpc - 1) / wpc;
+      const uint32_t slots = pl.cta_tile ? 1u : wpc;
+      uint64_t grid = (ntiles * c.members.size() + slots - 1) / slots;
       const uint64_t cap = (uint64_t)b->ctx->num_sms * 16;
       pl.grid = (uint32_t)std::max<uint64_t>(1, std::min(grid, cap));
       pl.rev = rev ? 1u : 0u;
@@ -111,7 +114,7 @@ void plan_class(qpe_batch* b, BatchClass& c) {
 size_t plans_smem(const qpe_batch* b, const BatchClass& c) {
   size_t m = 48 * 1024;
   for (const PassLaunch& pl : c.plans)
-    m = std::max(m, pass_stage_elems(pl.pass, pl.Ca, pl.Cb, pl.W) * b->esz * pl.warps_per_cta);
+    m = std::max(m, pass_stage_elems(pl.pass, pl.Ca, pl.Cb, pl.W) * b->esz * (pl.cta_tile ? 1 : pl.warps_per_cta));
   return m;
 }
 
@@ -129,7 +132,7 @@ void tune_class(qpe_batch* b, BatchClass& c) {
   uint32_t bw = 1, bwpc = 4;
   for (uint32_t W : {1u, 2u, 4u, 8u}) {
     if ((uint64_t)W * 2 > c.shape->hp.Cb && W > 1) continue;
-    for (uint32_t wpc : {2u, 4u, 8u}) {
+    for (uint32_t wpc : {0u, 2u, 4u, 8u}) {  // 0: one tile per CTA
       c.W = W;
       c.wpc = wpc;
       plan_class(b, c);

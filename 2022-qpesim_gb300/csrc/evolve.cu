@@ -17,6 +17,7 @@
 
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <stdint.h>
 
 #include "kernels.h"
@@ -39,13 +40,18 @@ __device__ __forceinline__ void async_copy(C2* dst, const C2* src) {
 //   PASS_COL: tile = W consecutive columns, stage[e * W + w] = block[e][b0 + w]
 //   PASS_ROW: tile = one row,               stage[e]         = block[a][e]
 //   PASS_MIX: tile = columns (b01, b10),    stage[e * 2 + w] = block[e][w ? b10 : b01]
-template <typename R, class A, int PT>
+//
+// CT: a whole CTA shares one tile (its threads split each term's entries, a CTA
+// barrier between terms); otherwise every warp owns its own tile.
+template <typename R, class A, int PT, bool CT>
 __global__ void k_pass(PassLaunch pl) {
   using C2 = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t warp = threadIdx.x >> 5;
-  const uint32_t wpc = blockDim.x >> 5;
+  const uint32_t lane = CT ? threadIdx.x : (threadIdx.x & 31);  // thread index within the tile
+  const uint32_t tpt = CT ? blockDim.x : 32u;                    // threads per tile
+  const uint32_t warp = CT ? 0u : (threadIdx.x >> 5);            // tile slot within the CTA
+  const uint32_t wpc = CT ? 1u : (blockDim.x >> 5);              // tile slots per CTA
+  using Sync = typename std::conditional<CT, CtaSync, WarpSync>::type;
   const uint32_t Ca = pl.Ca, Cb = pl.Cb;
   const uint32_t W = (PT == PASS_COL) ? pl.W : (PT == PASS_ROW ? 1u : 2u);
   const uint32_t L = (PT == PASS_ROW) ? Cb : Ca;
@@ -81,26 +87,26 @@ __global__ void k_pass(PassLaunch pl) {
       return (uint64_t)e * Cb + (w ? b10 : b01);
     };
     const uint32_t nst = L * W;
-    for (uint32_t i = lane; i < nst; i += 32)
+    for (uint32_t i = lane; i < nst; i += tpt)
       if ((i & (W - 1)) < nl) async_copy(st + i, blk + goff(i));
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
-    __syncwarp();
+    Sync()();
     if (PT == PASS_MIX) {
-      run_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, lane, 32, true, parb,
+      run_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, lane, tpt, true, parb,
                         [&](uint32_t a) -> C2& { return st[2 * a]; },
-                        [&](uint32_t a) -> C2& { return st[2 * a + 1]; }, icoef);
+                        [&](uint32_t a) -> C2& { return st[2 * a + 1]; }, icoef, Sync());
     } else {
       // Lane l owns line l % W and walks entries l / W, l / W + 32 / W, ...
       const uint32_t w = lane & (W - 1);
       const bool active = w < nl;
       const uint32_t line = (PT == PASS_COL) ? b0 + w : row;
       const uint32_t lstr = active ? __ldg(((PT == PASS_COL) ? pl.strB : pl.strA) + line) : 0u;
-      run_line_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, L, lane >> logW, 32 >> logW,
-                         active, lstr, [&](uint32_t e) -> C2& { return st[(e << logW) + w]; }, icoef);
+      run_line_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, L, lane >> logW, tpt >> logW,
+                         active, lstr, [&](uint32_t e) -> C2& { return st[(e << logW) + w]; }, icoef, Sync());
     }
-    for (uint32_t i = lane; i < nst; i += 32)
+    for (uint32_t i = lane; i < nst; i += tpt)
       if ((i & (W - 1)) < nl) blk[goff(i)] = st[i];
-    __syncwarp();
+    Sync()();
   }
 }
 
@@ -110,17 +116,22 @@ size_t pass_stage_elems(const Pass& pass, uint32_t Ca, uint32_t Cb, uint32_t W) 
   return (size_t)Ca * 2;
 }
 
-template <typename R, class A>
-static cudaError_t launch_typed(const PassLaunch& pl, cudaStream_t s) {
+template <typename R, class A, bool CT>
+static cudaError_t launch_ct(const PassLaunch& pl, cudaStream_t s) {
   using C2 = typename Cx<R>::T;
-  const size_t smem = pass_stage_elems(pl.pass, pl.Ca, pl.Cb, pl.W) * sizeof(C2) * pl.warps_per_cta;
-  const dim3 block(32 * pl.warps_per_cta);
+  const size_t smem = pass_stage_elems(pl.pass, pl.Ca, pl.Cb, pl.W) * sizeof(C2) * (CT ? 1 : pl.warps_per_cta);
+  const dim3 block(CT ? kCtaTileThreads : 32 * pl.warps_per_cta);
   switch (pl.pass.type) {
-    case PASS_COL: k_pass<R, A, PASS_COL><<<pl.grid, block, smem, s>>>(pl); break;
-    case PASS_ROW: k_pass<R, A, PASS_ROW><<<pl.grid, block, smem, s>>>(pl); break;
-    default: k_pass<R, A, PASS_MIX><<<pl.grid, block, smem, s>>>(pl); break;
+    case PASS_COL: k_pass<R, A, PASS_COL, CT><<<pl.grid, block, smem, s>>>(pl); break;
+    case PASS_ROW: k_pass<R, A, PASS_ROW, CT><<<pl.grid, block, smem, s>>>(pl); break;
+    default: k_pass<R, A, PASS_MIX, CT><<<pl.grid, block, smem, s>>>(pl); break;
   }
   return cudaGetLastError();
+}
+
+template <typename R, class A>
+static cudaError_t launch_typed(const PassLaunch& pl, cudaStream_t s) {
+  return pl.cta_tile ? launch_ct<R, A, true>(pl, s) : launch_ct<R, A, false>(pl, s);
 }
 
 cudaError_t launch_pass(const PassLaunch& pl, int dtype, cudaStream_t s) {
@@ -131,14 +142,21 @@ cudaError_t launch_pass(const PassLaunch& pl, int dtype, cudaStream_t s) {
   return launch_typed<float, Fast<float>>(pl, s);
 }
 
+template <typename R, class A, bool CT>
+static cudaError_t configure_ct(size_t smem) {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_pass<R, A, PASS_COL, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+    return e;
+  if ((e = cudaFuncSetAttribute(k_pass<R, A, PASS_ROW, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+    return e;
+  return cudaFuncSetAttribute(k_pass<R, A, PASS_MIX, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 template <typename R, class A>
 static cudaError_t configure_typed(size_t smem) {
-  cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_pass<R, A, PASS_COL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-    return e;
-  if ((e = cudaFuncSetAttribute(k_pass<R, A, PASS_ROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-    return e;
-  return cudaFuncSetAttribute(k_pass<R, A, PASS_MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = configure_ct<R, A, false>(smem);
+  if (e) return e;
+  return configure_ct<R, A, true>(smem);
 }
 
 // The shared-memory limit is a property of the kernel, not of one launch or one

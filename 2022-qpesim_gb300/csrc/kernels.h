@@ -46,7 +46,11 @@ struct PassLaunch {
   void* const* works;
   const double2* icoef;
   uint32_t nmem, nops;
+  // 1: one tile per CTA of kCtaTileThreads threads that split every term's
+  // entries (long tables); 0: one tile per warp.
+  uint32_t cta_tile;
 };
+constexpr uint32_t kCtaTileThreads = 128;
 size_t pass_stage_elems(const Pass& pass, uint32_t Ca, uint32_t Cb, uint32_t W);
 cudaError_t launch_pass(const PassLaunch& pl, int dtype, cudaStream_t s);
 cudaError_t launch_snapshot(const void* work, void* state, uint64_t block_elems, const int* d_k, int dtype,

@@ -157,6 +157,15 @@ __device__ __forceinline__ void diag_update(C2& v, const Coef4<R>& k) {
   v.y = xi;
 }
 
+// The barrier between consecutive terms of a tile: the warp's, or the CTA's when
+// a whole CTA shares one tile.
+struct WarpSync {
+  __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+struct CtaSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+
 __device__ __forceinline__ bool cond_ok(uint32_t line_str, const DevOp& op) {
   uint32_t m = 0;
   if (op.ncond > 0) m |= 1u << op.cb0;
@@ -172,11 +181,12 @@ __device__ __forceinline__ bool cond_ok(uint32_t line_str, const DevOp& op) {
 // coefficients and this lane's first table entry are loaded while the current
 // term computes, so the chain of dependent terms pays shared-memory latency
 // rather than the latency of the metadata loads.
-template <typename R, class A, bool G = true, class Elem>
+template <typename R, class A, bool G = true, class Elem, class Sync = WarpSync>
 __device__ __forceinline__ void run_line_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
                                              const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1, bool rev,
                                              uint32_t L, uint32_t jl, uint32_t jstep, bool active, uint32_t lstr,
-                                             Elem elem, const double2* __restrict__ icoef = nullptr) {
+                                             Elem elem, const double2* __restrict__ icoef = nullptr,
+                                             Sync sync = Sync()) {
   const uint32_t n = op1 - op0;
   if (n == 0) return;
   auto at = [&](uint32_t i) { return rev ? op1 - 1 - i : op0 + i; };
@@ -210,7 +220,7 @@ __device__ __forceinline__ void run_line_ops(const DevOp* __restrict__ ops, cons
         for (uint32_t e = jl; e < L; e += jstep) diag_update<A>(elem(e), op.k);
       }
     }
-    __syncwarp();
+    sync();
     op = opn;
     first = firstn;
   }
@@ -220,11 +230,12 @@ __device__ __forceinline__ void run_line_ops(const DevOp* __restrict__ ops, cons
 // (reverse order when `rev`): entry (a01 | par, a10) pairs left(a01) with
 // right(a10), parity adding the beta pair's parity parb
 // (cpp/time_evolution_over_terms.hpp:774). Pipelined as run_line_ops.
-template <typename R, class A, bool G = true, class Left, class Right>
+template <typename R, class A, bool G = true, class Left, class Right, class Sync = WarpSync>
 __device__ __forceinline__ void run_mix_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
                                             const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1, bool rev,
                                             uint32_t jl, uint32_t jstep, bool active, uint32_t parb, Left left,
-                                            Right right, const double2* __restrict__ icoef = nullptr) {
+                                            Right right, const double2* __restrict__ icoef = nullptr,
+                                            Sync sync = Sync()) {
   const uint32_t n = op1 - op0;
   if (n == 0) return;
   auto at = [&](uint32_t i) { return rev ? op1 - 1 - i : op0 + i; };
@@ -250,7 +261,7 @@ __device__ __forceinline__ void run_mix_ops(const DevOp* __restrict__ ops, const
         x = xn;
       }
     }
-    __syncwarp();
+    sync();
     op = opn;
     first = firstn;
   }
