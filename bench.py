@@ -77,6 +77,18 @@ WORKLOADS["learned-n12"] = dict(WORKLOADS["learned-n20"], n=12, N=6, P=8, train=
                                                  "8 held-out seeds, 8 ancilla qubits")
 DEFAULT_WORKLOAD = "plain-n16"
 
+# DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum +
+# dram__bytes_write.sum) from the ncu captures summarised under profiles/.
+MEASURED_TRAFFIC = {
+    "plain-n16": (495_872 + 1_024, "k_resident, cluster of 16: one launch runs every power; the capture of a "
+                                   "2-power launch read the block and the program once (0.50 MB) and wrote 1 KB, "
+                                   "the snapshots staying in L2 (profiles/k_resident_cluster16_plain_n16.md)"),
+    "precision-n24": (6_863_275, "k_pass MIX launch, one tile per CTA: the 6.8 MB working block read once, cold "
+                                 "cache under ncu (profiles/k_pass_precision_n24.md)"),
+    "batched-256": (28_600_000, "k_pass MIX launch: 3.57 MB for the 32-instance draw, scaled by the 8x members "
+                                "per launch (profiles/k_pass_batched32.md)"),
+}
+
 
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
@@ -333,6 +345,8 @@ def run_ours(args, w, rank, ws, local):
         line["config"]["powers_evolved"] = npow
     if args.precision:
         line["config"]["precision_override"] = args.precision
+    if args.workload in MEASURED_TRAFFIC:
+        line["roofline"]["traffic"], line["roofline"]["traffic_note"] = MEASURED_TRAFFIC[args.workload]
     if w.get("check_c128") and not args.powers:
         line["precision_check"] = precision_check(q, w, seg, st, prog, block0, local)
     if rank == 0 and not args.no_cpu_baseline:
@@ -517,6 +531,8 @@ def run_batch(args, w, rank, ws, local):
         "gpu_launches": int(info["launches_per_run"]) * args.steps,
         "clocks": clk,
     }
+    if args.workload in MEASURED_TRAFFIC:
+        line["roofline"]["traffic"], line["roofline"]["traffic_note"] = MEASURED_TRAFFIC[args.workload]
     if rank == 0 and not args.no_cpu_baseline:
         r, cores, sample = cpu_baseline_batch(q, w, terms)
         line["cpu_baseline"] = {"value": r, "unit": "touches/s", "cores": cores, "kind": "port", "sample": sample}
