@@ -40,28 +40,39 @@ __device__ __forceinline__ void group_ops(const DevOp* __restrict__ ops, const d
                                           uint32_t gthreads, Left left, Right right, Lstr lstr, Parb parb, Bar gbar) {
   using C2 = typename Cx<R>::T;
   const uint32_t n = op1 - op0;
+  if (n == 0) return;
   const uint32_t q = gt & 3u, slot = gt >> 2, nslots = gthreads >> 2;
-  const uint32_t W = 1u << logW;
+  // Items are (line w, entry j) with item = j * W + w; the slots step by
+  // nslots (a multiple of W), so a thread's line w is fixed for the tile and
+  // its line constants are loaded once.
+  const uint32_t w = slot & ((1u << logW) - 1);
+  const uint32_t j0 = slot >> logW, jstep = nslots >> logW;
+  const bool wvalid = w < nvalid;
+  const uint32_t my_lstr = (!mix && wvalid) ? lstr(w) : 0u;
+  const uint32_t my_parb = (mix && wvalid) ? parb(w) : 0u;
   for (uint32_t i = 0; i < n; ++i) {
     const OpR<R> op = load_op<R, G>(ops, coef, rev ? op1 - 1 - i : op0 + i);
     const DevOp& d = op.d;
     const Coef4<R>& k = op.k;
     const uint32_t per_line = d.kind == OPK_DIAG_ALL ? L : d.count;
-    const uint32_t nitems = per_line << logW;
-    for (uint32_t base = 0; base < nitems; base += nslots) {
-      const uint32_t item = base + slot;
-      const uint32_t w = item & (W - 1), j = item >> logW;
-      bool act = item < nitems && w < nvalid;
-      if (act && !mix && d.ncond) act = cond_ok(lstr(w), d);
+    const bool line_on = wvalid && (mix || d.ncond == 0 || cond_ok(my_lstr, d));
+    uint2 x = (d.kind == OPK_PAIR && j0 < per_line) ? ldm<G>(reinterpret_cast<const uint2*>(pool + d.tab) + j0)
+                                                    : make_uint2(0u, 0u);
+    // the same trip count for every thread of the group (the warp barrier below)
+    const uint32_t ntrips = (per_line + jstep - 1) / jstep;
+    for (uint32_t t = 0; t < ntrips; ++t) {
+      const uint32_t j = j0 + t * jstep;
+      const bool act = line_on && j < per_line;
+      uint2 xn = make_uint2(0u, 0u);
+      if (d.kind == OPK_PAIR && j + jstep < per_line) xn = ldm<G>(reinterpret_cast<const uint2*>(pool + d.tab) + j + jstep);
       R out = (R)0;
       C2* dst = nullptr;
       if (act) {
         if (d.kind == OPK_PAIR) {
-          const uint2 x = ldm<G>(reinterpret_cast<const uint2*>(pool + d.tab) + j);
           C2& lref = left(w, x.x & 0x7fffffffu);
           C2& rref = right(w, x.y);
           const C2 vl = lref, vr = rref;
-          const uint32_t par = (x.x >> 31) ^ parb(w);
+          const uint32_t par = (x.x >> 31) ^ my_parb;
           const R m0r = par ? k.o0r : k.e0r, m0i = par ? k.o0i : k.e0i;
           const R m1r = par ? k.o1r : k.e1r, m1i = par ? k.o1i : k.e1i;
           if (k.reduced) {
@@ -97,6 +108,7 @@ __device__ __forceinline__ void group_ops(const DevOp* __restrict__ ops, const d
         R* comp = reinterpret_cast<R*>(dst);
         comp[q & 1] = out;
       }
+      x = xn;
     }
     gbar();
   }
