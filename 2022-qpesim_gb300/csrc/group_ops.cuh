@@ -47,67 +47,80 @@ __device__ __forceinline__ void group_ops(const DevOp* __restrict__ ops, const d
   // its line constants are loaded once.
   const uint32_t w = slot & ((1u << logW) - 1);
   const uint32_t j0 = slot >> logW, jstep = nslots >> logW;
+  const uint32_t jshift = __ffs(jstep) - 1;  // jstep is a power of two
   const bool wvalid = w < nvalid;
   const uint32_t my_lstr = (!mix && wvalid) ? lstr(w) : 0u;
   const uint32_t my_parb = (mix && wvalid) ? parb(w) : 0u;
+  // Operand and result components of quad lane q for a pair (l, r) whose m00
+  // is real (c) and m01 imaginary (+-t), in R units from the amplitude start:
+  //   q0: l'.x = l.x c - r.y t    q1: l'.y = l.y c + r.x t
+  //   q2: r'.x = r.x c - l.y t    q3: r'.y = l.x t + r.y c
+  const bool x1_from_r = q == 2, x2_from_r = q != 2;
+  const uint32_t x1_comp = q == 1 ? 1u : 0u, x2_comp = q == 1 ? 0u : 1u;
+  const bool dst_r = q >= 2;
+  const uint32_t dst_comp = q & 1u;
   for (uint32_t i = 0; i < n; ++i) {
     const OpR<R> op = load_op<R, G>(ops, coef, rev ? op1 - 1 - i : op0 + i);
     const DevOp& d = op.d;
     const Coef4<R>& k = op.k;
     const uint32_t per_line = d.kind == OPK_DIAG_ALL ? L : d.count;
     const bool line_on = wvalid && (mix || d.ncond == 0 || cond_ok(my_lstr, d));
+    // this lane's coefficients for either parity (reduced pair) or the diagonal
+    R c1e, c1o, c2e, c2o;
+    if (d.kind == OPK_PAIR) {
+      const R c = k.e0r, te = k.e1i, to = k.o1i;  // m01 = i t, t = te (parity 0) or to (parity 1)
+      c1e = q == 3 ? te : c;
+      c1o = q == 3 ? to : c;
+      c2e = q == 3 ? c : ((q & 1) ? te : neg(te));
+      c2o = q == 3 ? c : ((q & 1) ? to : neg(to));
+    } else {
+      c1e = c1o = q ? k.e0i : k.e0r;
+      c2e = c2o = q ? k.e0r : neg(k.e0i);
+    }
     uint2 x = (d.kind == OPK_PAIR && j0 < per_line) ? ldm<G>(reinterpret_cast<const uint2*>(pool + d.tab) + j0)
                                                     : make_uint2(0u, 0u);
     // the same trip count for every thread of the group (the warp barrier below)
-    const uint32_t ntrips = (per_line + jstep - 1) / jstep;
+    const uint32_t ntrips = (per_line + jstep - 1) >> jshift;
     for (uint32_t t = 0; t < ntrips; ++t) {
       const uint32_t j = j0 + t * jstep;
       const bool act = line_on && j < per_line;
       uint2 xn = make_uint2(0u, 0u);
-      if (d.kind == OPK_PAIR && j + jstep < per_line) xn = ldm<G>(reinterpret_cast<const uint2*>(pool + d.tab) + j + jstep);
+      if (d.kind == OPK_PAIR && j + jstep < per_line)
+        xn = ldm<G>(reinterpret_cast<const uint2*>(pool + d.tab) + j + jstep);
       R out = (R)0;
-      C2* dst = nullptr;
+      R* dst = nullptr;
       if (act) {
         if (d.kind == OPK_PAIR) {
-          C2& lref = left(w, x.x & 0x7fffffffu);
-          C2& rref = right(w, x.y);
-          const C2 vl = lref, vr = rref;
+          R* lp = reinterpret_cast<R*>(&left(w, x.x & 0x7fffffffu));
+          R* rp = reinterpret_cast<R*>(&right(w, x.y));
           const uint32_t par = (x.x >> 31) ^ my_parb;
-          const R m0r = par ? k.o0r : k.e0r, m0i = par ? k.o0i : k.e0i;
-          const R m1r = par ? k.o1r : k.e1r, m1i = par ? k.o1i : k.e1i;
           if (k.reduced) {
-            // l'.re = lx c - ry t, l'.im = ly c + rx t, r'.re = rx c - ly t, r'.im = lx t + ry c
-            const R x1 = q == 0 ? vl.x : q == 1 ? vl.y : q == 2 ? vr.x : vl.x;
-            const R c1 = q == 3 ? m1i : m0r;
-            const R x2 = q == 0 ? vr.y : q == 1 ? vr.x : q == 2 ? vl.y : vr.y;
-            const R c2 = q == 3 ? m0r : ((q & 1) ? m1i : neg(m1i));
-            out = A::add(A::mul(x1, c1), A::mul(x2, c2));
+            const R x1 = (x1_from_r ? rp : lp)[x1_comp];
+            const R x2 = (x2_from_r ? rp : lp)[x2_comp];
+            out = A::add(A::mul(x1, par ? c1o : c1e), A::mul(x2, par ? c2o : c2e));
           } else {
             // l' = l m00 + r m01, r' = l m01 + r m00, every complex product (ac - bd, ad + bc)
+            const C2 vl = *reinterpret_cast<const C2*>(lp), vr = *reinterpret_cast<const C2*>(rp);
+            const R m0r = par ? k.o0r : k.e0r, m0i = par ? k.o0i : k.e0i;
+            const R m1r = par ? k.o1r : k.e1r, m1i = par ? k.o1i : k.e1i;
             const R ma_r = q < 2 ? m0r : m1r, ma_i = q < 2 ? m0i : m1i;  // multiplies l
             const R mb_r = q < 2 ? m1r : m0r, mb_i = q < 2 ? m1i : m0i;  // multiplies r
             const bool im = q & 1;
-            const R c1 = im ? ma_i : ma_r, c2 = im ? ma_r : neg(ma_i);
-            const R c3 = im ? mb_i : mb_r, c4 = im ? mb_r : neg(mb_i);
-            out = A::add(A::add(A::mul(vl.x, c1), A::mul(vl.y, c2)), A::add(A::mul(vr.x, c3), A::mul(vr.y, c4)));
+            const R g1 = im ? ma_i : ma_r, g2 = im ? ma_r : neg(ma_i);
+            const R g3 = im ? mb_i : mb_r, g4 = im ? mb_r : neg(mb_i);
+            out = A::add(A::add(A::mul(vl.x, g1), A::mul(vl.y, g2)), A::add(A::mul(vr.x, g3), A::mul(vr.y, g4)));
           }
-          C2& t = (q < 2) ? lref : rref;
-          dst = &t;
+          dst = (dst_r ? rp : lp) + dst_comp;
         } else if (q < 2) {
           const uint32_t e = d.kind == OPK_DIAG_LIST ? ldm<G>(pool + d.tab + j) : j;
-          C2& vref = left(w, e);
-          const C2 v = vref;
+          R* vp = reinterpret_cast<R*>(&left(w, e));
           // (vx c.r - vy c.i, vx c.i + vy c.r)
-          const R c1 = q ? k.e0i : k.e0r, c2 = q ? k.e0r : neg(k.e0i);
-          out = A::add(A::mul(v.x, c1), A::mul(v.y, c2));
-          dst = &vref;
+          out = A::add(A::mul(vp[0], c1e), A::mul(vp[1], c2e));
+          dst = vp + q;
         }
       }
       __syncwarp();
-      if (dst) {
-        R* comp = reinterpret_cast<R*>(dst);
-        comp[q & 1] = out;
-      }
+      if (dst) *dst = out;
       x = xn;
     }
     gbar();
