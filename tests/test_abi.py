@@ -44,3 +44,24 @@ def test_bf16_helpers_and_mlp_layout(q):
     assert r[6] == np.float32(1.0 + 2 ** -7)
     lay = L.param_layout()
     assert sum(int(np.prod(s)) for _, s in lay.values()) == 152336
+
+
+def test_learned_state_helpers_on_cpu(q):
+    import math
+
+    import numpy as np
+    L = q.learned_state
+    s = L.register_strings(4, 2, 2)
+    assert len(s) == 36 and len(set(int(x) for x in s)) == 36
+    assert all(bin(int(x) & 0xF).count("1") == 2 and bin(int(x) >> 4).count("1") == 2 for x in s)
+    # a Fejer peak: the ground bin is its lowest-energy local maximum, the sub-bin
+    # estimate recovers the energy, and the shot count to 1e-3 Ha is finite
+    n, t, E = 256, 0.05, -3.2
+    phi = (-E * t / (2 * math.pi)) % 1.0
+    j = np.arange(n)
+    d = (j / n - phi + 0.5) % 1.0 - 0.5
+    p = np.abs(np.sin(np.pi * n * d) / (n * np.sin(np.pi * d) + 1e-300)) ** 2
+    p /= p.sum()
+    j0 = L.ground_bin(p, t)
+    assert abs(L.subbin_energy(p, j0, n, t) - E) < 1e-6
+    assert L.shots_to_precision(p, j0, t, E) is not None
