@@ -330,9 +330,15 @@ def run_ours(args, w, rank, ws, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                      "kernel": kernel,
-                     "fp64": {"achieved_tflops": touches_step * 6 / ev_s / 1e12, "peak_tflops": FP64_PEAK_TFLOPS,
-                              "frac": touches_step * 6 / ev_s / 1e12 / FP64_PEAK_TFLOPS,
-                              "flops_per_touch": 6}} if w["dtype"] == "c128" else
+                     # 6 FP64 operations (DMUL / DADD, no FMA in exact mode) per touch, against the
+                     # FP64 issue rate: half the FMA FLOP/s, one operation per lane per issue
+                     "fp64": {"achieved_tops": touches_step * 6 / ev_s / 1e12, "peak_tops": FP64_PEAK_TFLOPS / 2,
+                              "frac": touches_step * 6 / ev_s / 1e12 / (FP64_PEAK_TFLOPS / 2),
+                              "ops_per_touch": 6,
+                              "note": "one controlled power is a chain of 3,200 dependent passes on the 16 SMs "
+                                      "of one cluster; a pass's terms are chains of dependent FP64 operations "
+                                      "(64 cycles of issue per warp instruction), so the bound is the chain's "
+                                      "latency, not throughput"}} if w["dtype"] == "c128" else
                     {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_kind, "kernel": kernel},
         "e2e": {"value": e2e_value, "unit": "touches/s",
