@@ -20,6 +20,12 @@ class BatchInfo(C.Structure):
                 ("amplitudes", C.c_uint64), ("launches_per_run", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class BatchClass(C.Structure):
+    _fields_ = [("num_orbitals", C.c_uint32), ("n_alpha", C.c_uint32), ("n_beta", C.c_uint32),
+                ("members", C.c_uint32), ("touches_per_power", C.c_uint64), ("ms_per_power", C.c_float),
+                ("tile_lines", C.c_uint32), ("warps_per_cta", C.c_uint32)]
+
+
 _PROTOS = {
     "qpe_batch_create": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p), C.c_uint32, C.c_int,
                                    C.POINTER(C.c_void_p)]),
@@ -30,6 +36,7 @@ _PROTOS = {
     "qpe_batch_run": (C.c_int, [C.c_void_p, C.c_int]),
     "qpe_batch_phase_probs": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_double)]),
     "qpe_batch_get_info": (C.c_int, [C.c_void_p, C.POINTER(BatchInfo)]),
+    "qpe_batch_class_info": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(BatchClass)]),
 }
 
 
@@ -71,6 +78,16 @@ class Batch:
         i = BatchInfo()
         N.check(self._lib.qpe_batch_get_info(self._h, C.byref(i)))
         return {f: getattr(i, f) for f, _ in BatchInfo._fields_}
+
+    def classes(self) -> list:
+        """Per class: orbitals, electrons per spin, members, touches per power
+        (all members) and the tuned time of one power of the class alone."""
+        out = []
+        for i in range(self.info["classes"]):
+            c = BatchClass()
+            N.check(self._lib.qpe_batch_class_info(self._h, i, C.byref(c)))
+            out.append({f: getattr(c, f) for f, _ in BatchClass._fields_})
+        return out
 
     def upload(self, i: int, host: np.ndarray, first: int = 0) -> None:
         a = np.ascontiguousarray(host, self.dtype)

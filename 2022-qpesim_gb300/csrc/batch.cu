@@ -35,6 +35,7 @@ struct BatchClass {
   DevBuf works_ptr, states_ptr;        // device arrays of per-member pointers
   DevBuf dk;
   uint32_t W = 0, wpc = 4;             // tile shape (lines per column tile, 0 = default; warps per CTA)
+  float tuned_ms = 0.f;                // one power of the class alone, best tile shape
   std::vector<PassLaunch> plans;       // one power: steps x sweeps of passes
 };
 
@@ -157,6 +158,7 @@ void tune_class(qpe_batch* b, BatchClass& c) {
   cudaEventDestroy(e1);
   c.W = bw;
   c.wpc = bwpc;
+  c.tuned_ms = best;
   plan_class(b, c);
 }
 
@@ -424,6 +426,23 @@ int qpe_batch_get_info(const qpe_batch* b, qpe_batch_info* info) {
   uint64_t amps = 0;
   for (uint32_t i = 0; i < b->n; ++i) amps += b->N * b->ld[i];
   info->amplitudes = amps;
+  return QPE_OK;
+}
+
+int qpe_batch_class_info(const qpe_batch* b, uint32_t cls, qpe_batch_class* out) {
+  if (!b || !out) return fail(QPE_ERR_INVALID, "null argument");
+  if (cls >= b->classes.size()) return fail(QPE_ERR_INVALID, "class index out of range");
+  const BatchClass& c = b->classes[cls];
+  const HostProgram& hp = c.shape->hp;
+  std::memset(out, 0, sizeof(*out));
+  out->num_orbitals = hp.M;
+  out->n_alpha = hp.na;
+  out->n_beta = hp.nb;
+  out->members = (uint32_t)c.members.size();
+  out->touches_per_power = hp.touches_per_power * c.members.size();
+  out->ms_per_power = c.tuned_ms;
+  out->tile_lines = c.W;
+  out->warps_per_cta = c.wpc;
   return QPE_OK;
 }
 

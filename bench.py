@@ -539,6 +539,16 @@ def run_batch(args, w, rank, ws, local):
     }
     if args.workload in MEASURED_TRAFFIC:
         line["roofline"]["traffic"], line["roofline"]["traffic_note"] = MEASURED_TRAFFIC[args.workload]
+    # throughput per instance size: each class (one size) timed alone by the autotuner
+    per_size = {}
+    for c in bt.classes():
+        ms = c["ms_per_power"]
+        per_size[str(2 * c["num_orbitals"])] = {
+            "instances": c["members"], "electrons": c["n_alpha"] + c["n_beta"],
+            "touches_per_power": c["touches_per_power"], "ms_per_power_alone": ms,
+            "touches_per_s_alone": c["touches_per_power"] / (ms / 1e3) if ms > 0 else None,
+            "tile": {"lines": c["tile_lines"], "warps_per_cta": c["warps_per_cta"]}}
+    line["per_size"] = per_size
     if rank == 0 and not args.no_cpu_baseline:
         r, cores, sample = cpu_baseline_batch(q, w, terms)
         line["cpu_baseline"] = {"value": r, "unit": "touches/s", "cores": cores, "kind": "port", "sample": sample}

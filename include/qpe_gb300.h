@@ -265,6 +265,16 @@ int qpe_batch_tune(qpe_batch* b);
 int qpe_batch_run(qpe_batch* b, int synchronize);
 int qpe_batch_phase_probs(qpe_batch* b, uint32_t instance, double* probs);
 int qpe_batch_get_info(const qpe_batch* b, qpe_batch_info* info);
+/* One class of a batch: instances of one program structure (one (M, Na, Nb)
+ * for the synthetic generator). ms_per_power is the tuned time of one power of
+ * the whole class run alone (measured by qpe_batch_tune; 0 before it). */
+typedef struct qpe_batch_class {
+  uint32_t num_orbitals, n_alpha, n_beta, members;
+  uint64_t touches_per_power;  /* summed over the class's members */
+  float ms_per_power;
+  uint32_t tile_lines, warps_per_cta;  /* the tuned tile shape (warps_per_cta 0: one tile per CTA) */
+} qpe_batch_class;
+int qpe_batch_class_info(const qpe_batch* b, uint32_t cls, qpe_batch_class* out);
 
 /* ---- QIFT without any allocation ------------------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device memory
