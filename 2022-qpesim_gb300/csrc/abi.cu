@@ -165,9 +165,9 @@ PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_opt
   // whose threads split every term's entries, so a term's chain is short.
   const uint64_t entries = binom((int)hp.M - 2, (int)(pass.type == PASS_ROW ? hp.nb : hp.na) - 1) *
                            (pass.type == PASS_COL ? W : 1);
-  pl.cta_tile = entries >= 64 ? 1u : 0u;
+  pl.cta_tile = entries >= 64 ? kCtaTileThreads : 0u;
   if (pl.cta_tile) {
-    wpc = kCtaTileThreads / 32;
+    wpc = pl.cta_tile / 32;
   } else if (esz == 16) {
     // complex128 tiles are bound by the SM's FP64 issue rate: spread the tiles
     // over the SMs first, then stack warps.
@@ -212,10 +212,13 @@ static uint32_t choose_lines(uint64_t lines, uint64_t nwarps, uint64_t entries) 
 }
 
 // Geometry of the resident kernel for cluster size K; false if it does not fit.
-// group: tiles processed by four-warp groups (k_resident_group), one stage per
-// group; otherwise by single warps (k_resident), one stage per warp.
+// mode (ResidentLaunch::group) 0: tiles processed by single warps (k_resident),
+// one stage per warp; 1: by four-warp groups (k_resident_group), one stage per
+// group; 2: column-pair tiles by four-warp groups, row and column tiles by
+// single warps, one stage per warp (a group uses its four warps' stages).
 static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K, ResidentLaunch& rl,
-                          ResidentInstance& ri, bool group = false) {
+                          ResidentInstance& ri, uint32_t mode = 0) {
+  const bool group = mode == 1;
   const HostProgram& hp = pr->hp;
   const size_t esz = st->esz;
   const uint64_t Ca = hp.Ca, Cb = hp.Cb;
@@ -240,11 +243,12 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
     ri.Wr = choose_lines(Rk, units, eb ? eb : 1);
     ri.Wc = choose_lines(Cb, (uint64_t)K * units, ea ? ea : 1);
     // at most 16 column pairs per tile: a thread's gather column is then fixed
-    ri.Wm = std::min<uint32_t>(16u, choose_lines(mixcount ? mixcount : 1, (uint64_t)K * units, ea ? ea : 1));
+    const uint32_t mix_units = mode == 2 ? wpc / 4 : units;
+    ri.Wm = std::min<uint32_t>(16u, choose_lines(mixcount ? mixcount : 1, (uint64_t)K * mix_units, ea ? ea : 1));
     uint64_t stage = 0;
     if (K > 1) {
       while (true) {
-        stage = std::max<uint64_t>(Ca * ri.Wc, 2 * Ca * ri.Wm);
+        stage = std::max<uint64_t>(Ca * ri.Wc, mode == 2 ? (2 * Ca * ri.Wm + 3) / 4 : 2 * Ca * ri.Wm);
         if (Rk * Cb * esz + units * stage * esz <= st->ctx->smem_optin || (ri.Wc == 1 && ri.Wm == 1)) break;
         if (ri.Wc > 1) ri.Wc /= 2;
         if (ri.Wm > 1 && 2 * Ca * ri.Wm > Ca * ri.Wc) ri.Wm /= 2;
@@ -259,7 +263,7 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
       rl.warps_per_cta = wpc;
       rl.stage_elems = (uint32_t)stage;
       rl.meta_smem = (uint32_t)with_meta;
-      rl.group = group ? 1u : 0u;
+      rl.group = mode;
       rl.smem_bytes = smem < 1024 ? 1024 : smem;
       return true;
     }
@@ -268,10 +272,10 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
 }
 
 static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint32_t first, uint32_t last,
-                         bool exact, bool in_place = false, bool group = false) {
+                         bool exact, bool in_place = false, uint32_t mode = 0) {
   ResidentLaunch rl;
   ResidentInstance ri{};
-  if (!plan_resident(pr, st, K, rl, ri, group))
+  if (!plan_resident(pr, st, K, rl, ri, mode))
     throw Error(QPE_ERR_UNSUPPORTED, "block does not fit the cluster's shared memory");
   ri.state = st->data.p;
   ri.pool = pr->pool.as<uint32_t>();
@@ -301,6 +305,11 @@ static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint3
 static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, uint32_t last, bool exact,
                          bool in_place = false);
 
+// ResidentLaunch::group of a resident strategy.
+static uint32_t resident_mode(uint32_t strategy) {
+  return strategy == QPE_STRATEGY_GROUP ? 1u : (strategy == QPE_STRATEGY_HYBRID ? 2u : 0u);
+}
+
 // Strategy for (program, state): explicit, or timed on one power per candidate.
 static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts, bool exact,
                             uint32_t& strategy, uint32_t& K) {
@@ -312,11 +321,11 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     K = 1;
     return;
   }
-  if (strategy == QPE_STRATEGY_CLUSTER || strategy == QPE_STRATEGY_GROUP) {
-    const bool grp = strategy == QPE_STRATEGY_GROUP;
+  if (strategy == QPE_STRATEGY_CLUSTER || strategy == QPE_STRATEGY_GROUP || strategy == QPE_STRATEGY_HYBRID) {
+    const uint32_t mode = resident_mode(strategy);
     if (K == 0) {
-      for (uint32_t c = grp ? 1 : 2; c <= 16 && !K; c *= 2)
-        if (plan_resident(pr, st, c, rl, ri, grp)) K = c;
+      for (uint32_t c = mode ? 1 : 2; c <= 16 && !K; c *= 2)
+        if (plan_resident(pr, st, c, rl, ri, mode)) K = c;
       if (!K) throw Error(QPE_ERR_UNSUPPORTED, "block does not fit a cluster of 16");
     }
     return;
@@ -341,7 +350,8 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
   std::vector<std::pair<uint32_t, uint32_t>> cands;
   for (uint32_t c = 1; c <= 16; c *= 2) {
     if (plan_resident(pr, st, c, rl, ri)) cands.push_back({c == 1 ? QPE_STRATEGY_RESIDENT : QPE_STRATEGY_CLUSTER, c});
-    if (plan_resident(pr, st, c, rl, ri, true)) cands.push_back({QPE_STRATEGY_GROUP, c});
+    if (plan_resident(pr, st, c, rl, ri, 1)) cands.push_back({QPE_STRATEGY_GROUP, c});
+    if (plan_resident(pr, st, c, rl, ri, 2)) cands.push_back({QPE_STRATEGY_HYBRID, c});
   }
   cands.push_back({QPE_STRATEGY_TILED, 0});
   if (cands.size() == 1) {
@@ -355,7 +365,7 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
       float ms = 0;
       auto run = [&]() {
         if (c.first == QPE_STRATEGY_TILED) evolve_tiled(st, pr, 1, 2, exact);
-        else run_resident(st, pr, c.second, 1, 2, exact, false, c.first == QPE_STRATEGY_GROUP);
+        else run_resident(st, pr, c.second, 1, 2, exact, false, resident_mode(c.first));
       };
       try {
         run();  // warm-up of this configuration
@@ -418,7 +428,7 @@ static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* 
   if (strategy == QPE_STRATEGY_TILED) {
     evolve_tiled(st, pr, first, last, exact, in_place);
   } else {
-    run_resident(st, pr, K, first, last, exact, in_place, strategy == QPE_STRATEGY_GROUP);
+    run_resident(st, pr, K, first, last, exact, in_place, resident_mode(strategy));
     QPE_CK(cudaStreamSynchronize(st->ctx->stream));
   }
 }
@@ -880,7 +890,7 @@ int qpe_evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts
   return guard([&] {
     check_state(st);
     if (!pr) throw Error(QPE_ERR_INVALID, "null program");
-    if (opts && opts->strategy > QPE_STRATEGY_GROUP) throw Error(QPE_ERR_INVALID, "unknown strategy");
+    if (opts && opts->strategy > QPE_STRATEGY_HYBRID) throw Error(QPE_ERR_INVALID, "unknown strategy");
     if (opts && opts->cluster_size && (opts->cluster_size > 16 || (opts->cluster_size & (opts->cluster_size - 1))))
       throw Error(QPE_ERR_INVALID, "cluster_size must be a power of two <= 16");
     if (opts && (opts->flags & ~(QPE_EVOLVE_FP64_CONTRACT | QPE_EVOLVE_IN_PLACE)))

@@ -91,7 +91,7 @@ void plan_class(qpe_batch* b, BatchClass& c) {
       if (pass.type == PASS_COL && c.W) pl.W = c.W;
       const size_t stage = pass_stage_elems(pass, pl.Ca, pl.Cb, pl.W) * b->esz;
       // wpc == 0 selects one tile per CTA (its threads split every term's entries)
-      pl.cta_tile = c.wpc == 0 ? 1u : 0u;
+      pl.cta_tile = c.wpc == 0 ? kCtaTileThreads : 0u;
       uint32_t wpc = c.wpc ? c.wpc : kCtaTileThreads / 32;
       while (!pl.cta_tile && wpc > 1 && stage * wpc > b->ctx->smem_optin) --wpc;
       pl.warps_per_cta = wpc;

@@ -120,7 +120,7 @@ template <typename R, class A, bool CT>
 static cudaError_t launch_ct(const PassLaunch& pl, cudaStream_t s) {
   using C2 = typename Cx<R>::T;
   const size_t smem = pass_stage_elems(pl.pass, pl.Ca, pl.Cb, pl.W) * sizeof(C2) * (CT ? 1 : pl.warps_per_cta);
-  const dim3 block(CT ? kCtaTileThreads : 32 * pl.warps_per_cta);
+  const dim3 block(CT ? pl.cta_tile : 32 * pl.warps_per_cta);
   switch (pl.pass.type) {
     case PASS_COL: k_pass<R, A, PASS_COL, CT><<<pl.grid, block, smem, s>>>(pl); break;
     case PASS_ROW: k_pass<R, A, PASS_ROW, CT><<<pl.grid, block, smem, s>>>(pl); break;

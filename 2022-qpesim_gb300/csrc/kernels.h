@@ -46,8 +46,8 @@ struct PassLaunch {
   void* const* works;
   const double2* icoef;
   uint32_t nmem, nops;
-  // 1: one tile per CTA of kCtaTileThreads threads that split every term's
-  // entries (long tables); 0: one tile per warp.
+  // > 0: one tile per CTA of this many threads (a multiple of 32), which split
+  // every term's entries (long tables); 0: one tile per warp.
   uint32_t cta_tile;
 };
 constexpr uint32_t kCtaTileThreads = 128;
@@ -93,6 +93,9 @@ struct ResidentLaunch {
   uint32_t stage_elems;           // per-warp stage (cluster > 1)
   uint32_t group;                 // 1: four-warp tile groups with quad-split updates
                                   //    (k_resident_group); stage_elems is then per group
+                                  // 2: column-pair passes by four-warp groups (whose
+                                  //    stage is their four warps' stages), row and
+                                  //    column passes by single warps (k_resident)
   uint32_t meta_smem;             // 1: term descriptors, index pool, passes and line
                                   //    strings are staged in every CTA's shared memory
   size_t smem_bytes;

@@ -82,10 +82,17 @@ size_t resident_meta_bytes(uint32_t nops, uint32_t pool_words, uint32_t npasses,
          (size_t)(Ca + Cb) * 4;
 }
 
+constexpr uint32_t kGroupWarps = 4;
+
 // MS: the program's metadata (term descriptors, index pool, passes, line strings)
 // is copied into every CTA's shared memory at the start, so that the term loop
 // reads it at shared-memory latency instead of through L1 / L2.
-template <typename R, class A, bool MS>
+// MG: column-pair (MIX) passes are processed by groups of kGroupWarps warps with
+// every update split over a quad of lanes (group_ops.cuh), as in
+// k_resident_group; group g stages its tile in the stages of its warps 4g ..
+// 4g + 3 (stage_elems is per warp). Row and column passes, whose many short
+// terms favour single warps, stay as below.
+template <typename R, class A, bool MS, bool MG>
 __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __restrict__ insts, uint32_t stage_elems) {
   using C2 = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -199,6 +206,46 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
             __syncwarp();
           }
         }
+      } else if constexpr (MG) {  // PASS_MIX by four-warp groups: Wm column pairs per group tile
+        const uint32_t gthreads = 32 * kGroupWarps, ngrp = wpc / kGroupWarps;
+        const uint32_t grp = warp / kGroupWarps, gt = threadIdx.x - grp * gthreads;
+        C2* gstage = blk + (size_t)Rk * Cb + (size_t)grp * kGroupWarps * stage_elems;
+        auto gbar = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(gthreads) : "memory"); };
+        auto no_lstr = [](uint32_t) { return 0u; };
+        const uint32_t W = I.Wm, logW = __ffs(W) - 1;
+        const uint32_t ntiles = (P.mixcount + W - 1) >> logW;
+        const uint2* __restrict__ mt = reinterpret_cast<const uint2*>(pool + P.mixtab);
+        for (uint32_t tile = grp * K + rank; tile < ntiles; tile += K * ngrp) {
+          const uint32_t t0 = tile << logW, nv = min(W, P.mixcount - t0);
+          auto pair_of = [&](uint32_t w) { return ldm<G>(mt + t0 + w); };
+          auto parb = [&](uint32_t w) { return pair_of(w).x >> 31; };
+          if (K == 1) {
+            auto left = [&](uint32_t w, uint32_t a) -> C2& {
+              return blk[(size_t)a * Cb + (pair_of(w).x & 0x7fffffffu)];
+            };
+            auto right = [&](uint32_t w, uint32_t a) -> C2& { return blk[(size_t)a * Cb + pair_of(w).y]; };
+            group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, logW, nv, true, gt, gthreads, left, right,
+                               no_lstr, parb, gbar);
+          } else {
+            // element i: row i >> (logW + 1), column pair (i >> 1) & (W - 1), side i & 1; with
+            // gthreads a multiple of 2W a thread's column is the same for all its elements
+            const uint32_t mysel = gt & (2 * W - 1);
+            const uint2 myq = ((mysel >> 1) < nv) ? pair_of(mysel >> 1) : make_uint2(0u, 0u);
+            const uint32_t mycol = (mysel & 1) ? myq.y : (myq.x & 0x7fffffffu);
+            auto ok = [&](uint32_t) { return (mysel >> 1) < nv; };
+            auto remote = [&](uint32_t i) { return at(i >> (logW + 1), mycol); };
+            auto local = [&](uint32_t i) { return gstage + i; };
+            const uint32_t n2 = Ca << (logW + 1);
+            group_copy<C2, kGatherDepth>(n2, gt, gthreads, ok, remote, local);
+            gbar();
+            auto left = [&](uint32_t w, uint32_t a) -> C2& { return gstage[(a << (logW + 1)) + 2 * w]; };
+            auto right = [&](uint32_t w, uint32_t a) -> C2& { return gstage[(a << (logW + 1)) + 2 * w + 1]; };
+            group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, logW, nv, true, gt, gthreads, left, right,
+                               no_lstr, parb, gbar);
+            group_copy<C2, kGatherDepth>(n2, gt, gthreads, ok, local, remote);
+            gbar();
+          }
+        }
       } else {  // PASS_MIX: Wm column pairs per tile
         const uint32_t W = I.Wm, logW = __ffs(W) - 1, w = lane & (W - 1);
         const uint32_t jl = lane >> logW, jstep = 32 >> logW;
@@ -250,7 +297,6 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
 // a term's FP64 work is spread over the four FP64 units of the SM instead of
 // one. Tiles (rows, columns or column pairs) go to the cluster's groups
 // round-robin; stage_elems is per group.
-constexpr uint32_t kGroupWarps = 4;
 
 template <typename R, class A, bool MS>
 __global__ void __launch_bounds__(512) k_resident_group(const ResidentInstance* __restrict__ insts,
@@ -418,7 +464,8 @@ static cudaError_t launch_res(const ResidentLaunch& rl, cudaStream_t s) {
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  auto kern = rl.group ? k_resident_group<R, A, MS> : k_resident<R, A, MS>;
+  auto kern = rl.group == 1 ? k_resident_group<R, A, MS>
+                            : (rl.group == 2 ? k_resident<R, A, MS, true> : k_resident<R, A, MS, false>);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rl.smem_bytes);
   if (e) return e;
   if (rl.cluster > 8) {
@@ -444,7 +491,9 @@ cudaError_t launch_resident(const ResidentLaunch& rl, int dtype, int exact, cuda
 
 template <typename R, class A, bool MS>
 static cudaError_t carveout_t(int percent) {
-  cudaError_t e = cudaFuncSetAttribute(k_resident<R, A, MS>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+  cudaError_t e = cudaFuncSetAttribute(k_resident<R, A, MS, false>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+  if (e) return e;
+  e = cudaFuncSetAttribute(k_resident<R, A, MS, true>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
   if (e) return e;
   return cudaFuncSetAttribute(k_resident_group<R, A, MS>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
 }

@@ -143,8 +143,10 @@ class DeviceState:
         """strategy: 0 auto (autotuned per program), 1 one CTA resident in shared
         memory, 2 a cluster of cluster_size CTAs (0: smallest that fits), 3
         global-memory tile passes, 4 a cluster whose tiles are processed by
-        four-warp groups with every update split over four lanes. fp64_contract allows FMAs in complex128
-        (within 1e-12 of the reference instead of bit-identical)."""
+        four-warp groups with every update split over four lanes, 5 a cluster
+        whose column-pair tiles are processed as in 4 and row and column tiles
+        as in 2. fp64_contract allows FMAs in complex128 (within 1e-12 of the
+        reference instead of bit-identical)."""
         opts = N.EvolveOpts(strategy, first_power, last_power, cluster_size,
                             N.QPE_EVOLVE_FP64_CONTRACT if fp64_contract else 0, 0)
         N.check(self._lib.qpe_evolve(self._h, program._h, C.byref(opts)))
@@ -166,7 +168,8 @@ class DeviceState:
         return p
 
     def last_strategy(self) -> tuple:
-        """(strategy, cluster size) of the last evolve: 1 resident, 2 cluster, 3 tiled, 4 grouped cluster."""
+        """(strategy, cluster size) of the last evolve: 1 resident, 2 cluster, 3 tiled, 4 grouped cluster,
+        5 cluster with grouped column-pair tiles."""
         s, k = C.c_uint32(), C.c_uint32()
         N.check(self._lib.qpe_state_last_strategy(self._h, C.byref(s), C.byref(k)))
         return s.value, k.value

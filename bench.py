@@ -303,10 +303,11 @@ def run_ours(args, w, rank, ws, local):
         launches = args.steps * (npow * (info["num_passes_per_power"] + 2) + 1 + 2 + 1)
     else:
         kernel = (f"{'k_resident_group' if strat == 4 else 'k_resident'} (whole evolution in one launch, "
-                  f"cluster of {kc} CTA(s))")
+                  f"cluster of {kc} CTA(s){', column pairs by four-warp groups' if strat == 5 else ''})")
         launches = args.steps * (1 + 2)
     strategy_name = {1: "resident (one CTA)", 2: f"cluster of {kc} CTAs", 3: "tiled passes",
-                     4: f"cluster of {kc} CTAs, four-warp tile groups"}.get(strat, "?")
+                     4: f"cluster of {kc} CTAs, four-warp tile groups",
+                     5: f"cluster of {kc} CTAs, column-pair tiles by four-warp groups"}.get(strat, "?")
     line = {
         "metric": "amplitude-term updates/s per Trotter step",
         "value": value,
@@ -747,7 +748,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--strategy", type=int, default=0,
-                    help="0 auto, 1 one-CTA resident, 2 cluster, 3 tiled, 4 cluster with four-warp groups")
+                    help="0 auto, 1 one-CTA resident, 2 cluster, 3 tiled, 4 cluster with four-warp groups, "
+                         "5 cluster with column pairs by four-warp groups")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per cluster for --strategy 2 (0: smallest)")
     ap.add_argument("--powers", type=int, default=0,
                     help="evolve only the first K controlled powers (profiling runs; not a workload's figure)")

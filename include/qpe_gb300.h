@@ -208,6 +208,8 @@ int qpe_state_zero(qpe_state* st);
 #define QPE_STRATEGY_TILED 3    /* L2-resident block, shared-memory tile passes */
 #define QPE_STRATEGY_GROUP 4    /* as CLUSTER (cluster_size 1..16), tiles processed by four-warp
                                    groups with every update split over four lanes */
+#define QPE_STRATEGY_HYBRID 5   /* as CLUSTER (cluster_size 1..16): column-pair passes as GROUP,
+                                   row and column passes as CLUSTER */
 
 /* complex128 only: allow fused multiply-adds. Results then differ from the
  * reference's rounding by a few ulps per update (within 1e-12 of it) instead of
