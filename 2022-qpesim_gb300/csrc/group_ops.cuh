@@ -127,6 +127,115 @@ __device__ __forceinline__ void group_ops(const DevOp* __restrict__ ops, const d
   }
 }
 
+// The terms of a column-pair (MIX) pass on a group tile of W column pairs: the
+// lean form of group_ops for the inline pair matrices every term of the
+// reference's getters has (m00 = c for both parities, m01 = i t for parity 0
+// and -i t for parity 1). With t_p the parity's t, the four results of a pair
+// (l, r) are
+//   q0: l'.x = l.x c + r.y (-t_p)   q1: l'.y = l.y c + r.x t_p
+//   q2: r'.x = r.x c + l.y (-t_p)   q3: r'.y = r.y c + l.x t_p
+// which are updateStateVector's (cpp/time_evolution_over_terms.hpp:565-589)
+// expressions bit for bit: a - b*t is a + b*(-t) exactly, and the sum of two
+// products does not depend on their order. So lane q reads component x1 (the
+// one it writes) and x2, and does two multiplications and one addition.
+//
+// The next term's descriptor and first table entry are loaded while the
+// current term runs, so a term's critical path is its operand loads, its three
+// FP64 operations, the store and the group barrier. A term with a general
+// matrix (a coefficient record) takes the general quad update of group_ops.
+template <typename R, class A, bool G, class Left, class Right, class Parb, class Bar>
+__device__ __forceinline__ void group_mix_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
+                                              const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1,
+                                              bool rev, uint32_t logW, uint32_t nvalid, uint32_t gt,
+                                              uint32_t gthreads, Left left, Right right, Parb parb, Bar gbar) {
+  using C2 = typename Cx<R>::T;
+  const uint32_t n = op1 - op0;
+  if (n == 0) return;
+  const uint32_t q = gt & 3u, slot = gt >> 2, nslots = gthreads >> 2;
+  const uint32_t w = slot & ((1u << logW) - 1);
+  const uint32_t j0 = slot >> logW, jstep = nslots >> logW;
+  const uint32_t jshift = __ffs(jstep) - 1;  // jstep is a power of two
+  const bool wvalid = w < nvalid;
+  const uint32_t my_parb = wvalid ? parb(w) : 0u;
+  const bool side1 = q >= 2;                  // x1 (and the result) on the right amplitude
+  const uint32_t comp1 = q & 1u, comp2 = comp1 ^ 1u;
+  const uint32_t sflip = comp1 ^ 1u;          // q0, q2 multiply x2 by -t_p
+  auto desc = [&](uint32_t i, uint4& a, uint4& b) {
+    const uint4* src = reinterpret_cast<const uint4*>(ops + (rev ? op1 - 1 - i : op0 + i));
+    a = ldm<G>(src);
+    b = ldm<G>(src + 1);
+  };
+  auto entry = [&](uint32_t tab, uint32_t count, uint32_t j) {
+    return j < count ? ldm<G>(reinterpret_cast<const uint2*>(pool + tab) + j) : make_uint2(0u, 0u);
+  };
+  uint4 a, b;  // DevOp words: a = (tab, count, kind | ncond | cb0 | cb1, gen), b = (c0, c1)
+  desc(0, a, b);
+  uint2 x = entry(a.x, a.y, j0);
+  for (uint32_t i = 0; i < n; ++i) {
+    uint4 na = a, nb = b;
+    uint2 nx = make_uint2(0u, 0u);
+    if (i + 1 < n) {
+      desc(i + 1, na, nb);
+      nx = entry(na.x, na.y, j0);
+    }
+    const uint32_t tab = a.x, count = a.y;
+    const uint32_t ntrips = (count + jstep - 1) >> jshift;
+    if (a.w == OP_INLINE) {
+      const R c = (R)__hiloint2double((int)b.y, (int)b.x), t = (R)__hiloint2double((int)b.w, (int)b.z);
+      const R tn = neg(t);
+      for (uint32_t tr = 0; tr < ntrips; ++tr) {
+        const uint32_t j = j0 + tr * jstep;
+        const uint2 xn = entry(tab, count, j + jstep);
+        R out = (R)0;
+        R* dst = nullptr;
+        if (wvalid && j < count) {
+          R* lp = reinterpret_cast<R*>(&left(w, x.x & 0x7fffffffu));
+          R* rp = reinterpret_cast<R*>(&right(w, x.y));
+          const uint32_t par = (x.x >> 31) ^ my_parb;
+          dst = (side1 ? rp : lp) + comp1;
+          const R x1 = *dst, x2 = (side1 ? lp : rp)[comp2];
+          out = A::add(A::mul(x1, c), A::mul(x2, (par ^ sflip) ? tn : t));
+        }
+        __syncwarp();
+        if (dst) *dst = out;
+        x = xn;
+      }
+    } else {
+      // general matrix: l' = l m00 + r m01, r' = l m01 + r m00 (group_ops' general update)
+      const double2* cr = reinterpret_cast<const double2*>(coef + 8 * (size_t)a.w);
+      const double2 e0 = __ldg(cr), e1 = __ldg(cr + 1), o0 = __ldg(cr + 2), o1 = __ldg(cr + 3);
+      for (uint32_t tr = 0; tr < ntrips; ++tr) {
+        const uint32_t j = j0 + tr * jstep;
+        const uint2 xn = entry(tab, count, j + jstep);
+        R out = (R)0;
+        R* dst = nullptr;
+        if (wvalid && j < count) {
+          R* lp = reinterpret_cast<R*>(&left(w, x.x & 0x7fffffffu));
+          R* rp = reinterpret_cast<R*>(&right(w, x.y));
+          const uint32_t par = (x.x >> 31) ^ my_parb;
+          const C2 vl = *reinterpret_cast<const C2*>(lp), vr = *reinterpret_cast<const C2*>(rp);
+          const R m0r = (R)(par ? o0.x : e0.x), m0i = (R)(par ? o0.y : e0.y);
+          const R m1r = (R)(par ? o1.x : e1.x), m1i = (R)(par ? o1.y : e1.y);
+          const R ma_r = q < 2 ? m0r : m1r, ma_i = q < 2 ? m0i : m1i;  // multiplies l
+          const R mb_r = q < 2 ? m1r : m0r, mb_i = q < 2 ? m1i : m0i;  // multiplies r
+          const bool im = q & 1;
+          const R g1 = im ? ma_i : ma_r, g2 = im ? ma_r : neg(ma_i);
+          const R g3 = im ? mb_i : mb_r, g4 = im ? mb_r : neg(mb_i);
+          out = A::add(A::add(A::mul(vl.x, g1), A::mul(vl.y, g2)), A::add(A::mul(vr.x, g3), A::mul(vr.y, g4)));
+          dst = (q >= 2 ? rp : lp) + (q & 1);
+        }
+        __syncwarp();
+        if (dst) *dst = out;
+        x = xn;
+      }
+    }
+    gbar();
+    a = na;
+    b = nb;
+    x = nx;
+  }
+}
+
 }  // namespace qpe
 
 #endif  // QPE_GROUP_OPS_CUH_

@@ -211,7 +211,6 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
         const uint32_t grp = warp / kGroupWarps, gt = threadIdx.x - grp * gthreads;
         C2* gstage = blk + (size_t)Rk * Cb + (size_t)grp * kGroupWarps * stage_elems;
         auto gbar = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(gthreads) : "memory"); };
-        auto no_lstr = [](uint32_t) { return 0u; };
         const uint32_t W = I.Wm, logW = __ffs(W) - 1;
         const uint32_t ntiles = (P.mixcount + W - 1) >> logW;
         const uint2* __restrict__ mt = reinterpret_cast<const uint2*>(pool + P.mixtab);
@@ -224,8 +223,8 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
               return blk[(size_t)a * Cb + (pair_of(w).x & 0x7fffffffu)];
             };
             auto right = [&](uint32_t w, uint32_t a) -> C2& { return blk[(size_t)a * Cb + pair_of(w).y]; };
-            group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, logW, nv, true, gt, gthreads, left, right,
-                               no_lstr, parb, gbar);
+            group_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, logW, nv, gt, gthreads, left, right, parb,
+                                   gbar);
           } else {
             // element i: row i >> (logW + 1), column pair (i >> 1) & (W - 1), side i & 1; with
             // gthreads a multiple of 2W a thread's column is the same for all its elements
@@ -240,8 +239,8 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
             gbar();
             auto left = [&](uint32_t w, uint32_t a) -> C2& { return gstage[(a << (logW + 1)) + 2 * w]; };
             auto right = [&](uint32_t w, uint32_t a) -> C2& { return gstage[(a << (logW + 1)) + 2 * w + 1]; };
-            group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, logW, nv, true, gt, gthreads, left, right,
-                               no_lstr, parb, gbar);
+            group_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, logW, nv, gt, gthreads, left, right, parb,
+                                   gbar);
             group_copy<C2, kGatherDepth>(n2, gt, gthreads, ok, local, remote);
             gbar();
           }
@@ -418,8 +417,8 @@ __global__ void __launch_bounds__(512) k_resident_group(const ResidentInstance* 
                 return blk[(size_t)a * Cb + (pair_of(w).x & 0x7fffffffu)];
               };
               auto right = [&](uint32_t w, uint32_t a) -> C2& { return blk[(size_t)a * Cb + pair_of(w).y]; };
-              group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, logW, nv, true, gt, gthreads, left, right,
-                                 no_parity, parb, gbar);
+              group_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, logW, nv, gt, gthreads, left, right, parb,
+                                     gbar);
             } else {
               // element i: row i >> (logW + 1), column pair (i >> 1) & (W - 1), side i & 1; with
               // gthreads a multiple of 2W a thread's column is the same for all its elements
@@ -434,8 +433,8 @@ __global__ void __launch_bounds__(512) k_resident_group(const ResidentInstance* 
               gbar();
               auto left = [&](uint32_t w, uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w]; };
               auto right = [&](uint32_t w, uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w + 1]; };
-              group_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, logW, nv, true, gt, gthreads, left, right,
-                                 no_parity, parb, gbar);
+              group_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, logW, nv, gt, gthreads, left, right, parb,
+                                     gbar);
               group_copy<C2, kDepth>(n2, gt, gthreads, ok, local, remote);
               gbar();
             }
