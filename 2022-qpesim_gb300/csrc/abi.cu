@@ -256,7 +256,8 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
     }
     const size_t head = (size_t)(Rk * Cb * esz + units * stage * esz);
     const size_t smem = with_meta ? ((head + 15) & ~(size_t)15) + meta : head;
-    if (smem <= st->ctx->smem_optin) {
+    // the kernels' static shared memory (kResidentStaticSmem) comes on top
+    if (smem + kResidentStaticSmem <= st->ctx->smem_optin) {
       rl = ResidentLaunch{};
       rl.ninst = 1;
       rl.cluster = K;

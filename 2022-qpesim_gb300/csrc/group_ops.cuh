@@ -137,17 +137,26 @@ __device__ __forceinline__ void group_ops(const DevOp* __restrict__ ops, const d
 // which are updateStateVector's (cpp/time_evolution_over_terms.hpp:565-589)
 // expressions bit for bit: a - b*t is a + b*(-t) exactly, and the sum of two
 // products does not depend on their order. So lane q reads component x1 (the
-// one it writes) and x2, and does two multiplications and one addition.
+// one it writes) and x2, and does two multiplications and one addition; x2 is
+// the x1 of quad lane q ^ 3, so it comes by a shuffle and no lane reads an
+// element another lane writes.
 //
-// The next term's descriptor and first table entry are loaded while the
-// current term runs, so a term's critical path is its operand loads, its three
-// FP64 operations, the store and the group barrier. A term with a general
-// matrix (a coefficient record) takes the general quad update of group_ops.
+// A term is a chain through shared memory (load, three FP64 operations, store,
+// group barrier), so everything else is taken off that chain: terms go in
+// chunks of kMixChunk whose descriptors, table entries, coefficients and element
+// addresses are all loaded and computed before the chunk's first update. Lanes
+// without a pair in a warp that has some work on `scratch` (a group-private
+// element) instead of branching; a warp with no pair in a term skips it.
+// Passes with a term of more entries than the group has quads, or with a
+// general matrix (a coefficient record), take the term-by-term loop below.
+constexpr uint32_t kMixChunk = 4;
+
 template <typename R, class A, bool G, class Left, class Right, class Parb, class Bar>
 __device__ __forceinline__ void group_mix_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
                                               const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1,
                                               bool rev, uint32_t logW, uint32_t nvalid, uint32_t gt,
-                                              uint32_t gthreads, Left left, Right right, Parb parb, Bar gbar) {
+                                              uint32_t gthreads, Left left, Right right, Parb parb, Bar gbar,
+                                              typename Cx<R>::T* scratch) {
   using C2 = typename Cx<R>::T;
   const uint32_t n = op1 - op0;
   if (n == 0) return;
@@ -155,6 +164,7 @@ __device__ __forceinline__ void group_mix_ops(const DevOp* __restrict__ ops, con
   const uint32_t w = slot & ((1u << logW) - 1);
   const uint32_t j0 = slot >> logW, jstep = nslots >> logW;
   const uint32_t jshift = __ffs(jstep) - 1;  // jstep is a power of two
+  const uint32_t wj0 = ((gt & ~31u) >> 2) >> logW;  // smallest j0 of this thread's warp
   const bool wvalid = w < nvalid;
   const uint32_t my_parb = wvalid ? parb(w) : 0u;
   const bool side1 = q >= 2;                  // x1 (and the result) on the right amplitude
@@ -165,19 +175,65 @@ __device__ __forceinline__ void group_mix_ops(const DevOp* __restrict__ ops, con
     a = ldm<G>(src);
     b = ldm<G>(src + 1);
   };
+  // entry j of a table of `count` entries (clamped: lanes past the end read the last one)
   auto entry = [&](uint32_t tab, uint32_t count, uint32_t j) {
-    return j < count ? ldm<G>(reinterpret_cast<const uint2*>(pool + tab) + j) : make_uint2(0u, 0u);
+    return count ? ldm<G>(reinterpret_cast<const uint2*>(pool + tab) + min(j, count - 1)) : make_uint2(0u, 0u);
   };
+  // Fast path: every term inline with at most jstep entries (one trip).
+  bool fast = true;
+  for (uint32_t i = 0; i < n && fast; ++i) {
+    const uint4 d = ldm<G>(reinterpret_cast<const uint4*>(ops + op0 + i));
+    fast = d.w == OP_INLINE && d.y <= jstep;
+  }
+  if (fast) {
+    for (uint32_t i0 = 0; i0 < n; i0 += kMixChunk) {
+      R cc[kMixChunk], ss[kMixChunk];
+      R* dp[kMixChunk];
+      bool wact[kMixChunk];
+#pragma unroll
+      for (uint32_t k = 0; k < kMixChunk; ++k) {
+        cc[k] = ss[k] = (R)0;
+        dp[k] = reinterpret_cast<R*>(scratch);
+        wact[k] = false;
+        if (i0 + k < n) {
+          uint4 a, b;
+          desc(i0 + k, a, b);
+          const uint2 x = entry(a.x, a.y, j0);
+          const bool act = wvalid && j0 < a.y;
+          wact[k] = wj0 < a.y;
+          cc[k] = (R)__hiloint2double((int)b.y, (int)b.x);
+          const R t = (R)__hiloint2double((int)b.w, (int)b.z);
+          ss[k] = (((x.x >> 31) ^ my_parb ^ sflip) && act) ? neg(t) : t;
+          if (act) {
+            R* lp = reinterpret_cast<R*>(&left(w, x.x & 0x7fffffffu));
+            R* rp = reinterpret_cast<R*>(&right(w, x.y));
+            dp[k] = (side1 ? rp : lp) + comp1;
+          } else {
+            dp[k] = reinterpret_cast<R*>(scratch) + comp1;
+          }
+        }
+      }
+#pragma unroll
+      for (uint32_t k = 0; k < kMixChunk; ++k) {
+        if (i0 + k < n) {
+          if (wact[k]) {
+            const R x1 = *dp[k];
+            const R x2 = __shfl_xor_sync(0xffffffffu, x1, 3);
+            *dp[k] = A::add(A::mul(x1, cc[k]), A::mul(x2, ss[k]));
+          }
+          gbar();
+        }
+      }
+    }
+    return;
+  }
   uint4 a, b;  // DevOp words: a = (tab, count, kind | ncond | cb0 | cb1, gen), b = (c0, c1)
   desc(0, a, b);
   uint2 x = entry(a.x, a.y, j0);
   for (uint32_t i = 0; i < n; ++i) {
-    uint4 na = a, nb = b;
-    uint2 nx = make_uint2(0u, 0u);
-    if (i + 1 < n) {
-      desc(i + 1, na, nb);
-      nx = entry(na.x, na.y, j0);
-    }
+    uint4 na, nb;
+    desc(min(i + 1, n - 1), na, nb);
+    const uint2 nx = entry(na.x, na.y, j0);
     const uint32_t tab = a.x, count = a.y;
     const uint32_t ntrips = (count + jstep - 1) >> jshift;
     if (a.w == OP_INLINE) {
@@ -186,18 +242,17 @@ __device__ __forceinline__ void group_mix_ops(const DevOp* __restrict__ ops, con
       for (uint32_t tr = 0; tr < ntrips; ++tr) {
         const uint32_t j = j0 + tr * jstep;
         const uint2 xn = entry(tab, count, j + jstep);
-        R out = (R)0;
-        R* dst = nullptr;
-        if (wvalid && j < count) {
-          R* lp = reinterpret_cast<R*>(&left(w, x.x & 0x7fffffffu));
-          R* rp = reinterpret_cast<R*>(&right(w, x.y));
+        if (wj0 + tr * jstep < count) {  // some lane of the warp has a pair
+          const bool act = wvalid && j < count;
+          R* lp = act ? reinterpret_cast<R*>(&left(w, x.x & 0x7fffffffu)) : reinterpret_cast<R*>(scratch);
+          R* rp = act ? reinterpret_cast<R*>(&right(w, x.y)) : reinterpret_cast<R*>(scratch);
           const uint32_t par = (x.x >> 31) ^ my_parb;
-          dst = (side1 ? rp : lp) + comp1;
+          R* dst = (side1 ? rp : lp) + comp1;
           const R x1 = *dst, x2 = (side1 ? lp : rp)[comp2];
-          out = A::add(A::mul(x1, c), A::mul(x2, (par ^ sflip) ? tn : t));
+          const R out = A::add(A::mul(x1, c), A::mul(x2, (par ^ sflip) ? tn : t));
+          __syncwarp();
+          *dst = out;
         }
-        __syncwarp();
-        if (dst) *dst = out;
         x = xn;
       }
     } else {

@@ -100,6 +100,9 @@ struct ResidentLaunch {
                                   //    strings are staged in every CTA's shared memory
   size_t smem_bytes;
 };
+// Upper bound of the resident kernels' static shared memory (a scratch element
+// per four-warp group).
+constexpr size_t kResidentStaticSmem = 256;
 // Bytes of shared memory the staged program metadata takes (ResidentLaunch::meta_smem).
 size_t resident_meta_bytes(uint32_t nops, uint32_t pool_words, uint32_t npasses, uint32_t Ca, uint32_t Cb);
 cudaError_t launch_resident(const ResidentLaunch& rl, int dtype, int exact, cudaStream_t s);

@@ -96,6 +96,8 @@ template <typename R, class A, bool MS, bool MG>
 __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __restrict__ insts, uint32_t stage_elems) {
   using C2 = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // one element per four-warp group for the lanes of group_mix_ops without a pair
+  __shared__ C2 scratch_s[16 / kGroupWarps];
   cg::cluster_group cl = cg::this_cluster();
   const uint32_t K = cl.num_blocks();
   const uint32_t rank = cl.block_rank();
@@ -224,7 +226,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
             };
             auto right = [&](uint32_t w, uint32_t a) -> C2& { return blk[(size_t)a * Cb + pair_of(w).y]; };
             group_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, logW, nv, gt, gthreads, left, right, parb,
-                                   gbar);
+                                   gbar, scratch_s + grp);
           } else {
             // element i: row i >> (logW + 1), column pair (i >> 1) & (W - 1), side i & 1; with
             // gthreads a multiple of 2W a thread's column is the same for all its elements
@@ -240,7 +242,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
             auto left = [&](uint32_t w, uint32_t a) -> C2& { return gstage[(a << (logW + 1)) + 2 * w]; };
             auto right = [&](uint32_t w, uint32_t a) -> C2& { return gstage[(a << (logW + 1)) + 2 * w + 1]; };
             group_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, logW, nv, gt, gthreads, left, right, parb,
-                                   gbar);
+                                   gbar, scratch_s + grp);
             group_copy<C2, kGatherDepth>(n2, gt, gthreads, ok, local, remote);
             gbar();
           }
@@ -302,6 +304,7 @@ __global__ void __launch_bounds__(512) k_resident_group(const ResidentInstance* 
                                                         uint32_t stage_elems) {
   using C2 = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ C2 scratch_s[16 / kGroupWarps];  // as in k_resident
   cg::cluster_group cl = cg::this_cluster();
   const uint32_t K = cl.num_blocks();
   const uint32_t rank = cl.block_rank();
@@ -418,7 +421,7 @@ __global__ void __launch_bounds__(512) k_resident_group(const ResidentInstance* 
               };
               auto right = [&](uint32_t w, uint32_t a) -> C2& { return blk[(size_t)a * Cb + pair_of(w).y]; };
               group_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, logW, nv, gt, gthreads, left, right, parb,
-                                     gbar);
+                                     gbar, scratch_s + grp);
             } else {
               // element i: row i >> (logW + 1), column pair (i >> 1) & (W - 1), side i & 1; with
               // gthreads a multiple of 2W a thread's column is the same for all its elements
@@ -434,7 +437,7 @@ __global__ void __launch_bounds__(512) k_resident_group(const ResidentInstance* 
               auto left = [&](uint32_t w, uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w]; };
               auto right = [&](uint32_t w, uint32_t a) -> C2& { return stage[(a << (logW + 1)) + 2 * w + 1]; };
               group_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, logW, nv, gt, gthreads, left, right, parb,
-                                     gbar);
+                                     gbar, scratch_s + grp);
               group_copy<C2, kDepth>(n2, gt, gthreads, ok, local, remote);
               gbar();
             }
