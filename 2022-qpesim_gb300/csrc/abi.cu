@@ -211,6 +211,41 @@ static uint32_t choose_lines(uint64_t lines, uint64_t nwarps, uint64_t entries) 
   return best;
 }
 
+// Geometry of k_resident_lean for cluster size K: three-warp groups (15, 12, 9,
+// 6 or 3 warps per CTA), one line or column pair per group tile, a stage of one
+// column pair (2 Ca elements) per group when K > 1.
+static bool plan_resident_lean(const qpe_program* pr, const qpe_state* st, uint32_t K, ResidentLaunch& rl,
+                               ResidentInstance& ri) {
+  const HostProgram& hp = pr->hp;
+  const size_t esz = st->esz;
+  const uint64_t Ca = hp.Ca, Cb = hp.Cb;
+  const uint64_t Rk = (Ca + K - 1) / K;
+  const size_t meta = resident_meta_bytes((uint32_t)hp.ops.size(), (uint32_t)hp.pool_words,
+                                          (uint32_t)hp.passes.size(), (uint32_t)Ca, (uint32_t)Cb);
+  const uint64_t stage = K > 1 ? 2 * Ca : 0;
+  for (int with_meta = 1; with_meta >= 0; --with_meta)
+    for (uint32_t wpc = 15; wpc >= 3; wpc -= 3) {
+      const size_t head = (size_t)(Rk * Cb * esz + (wpc / 3) * stage * esz);
+      const size_t smem = with_meta ? ((head + 15) & ~(size_t)15) + meta : head;
+      if (smem + kResidentStaticSmem > st->ctx->smem_optin) continue;
+      ri = ResidentInstance{};
+      ri.Ca = (uint32_t)Ca;
+      ri.Cb = (uint32_t)Cb;
+      ri.rows_per_cta = (uint32_t)Rk;
+      ri.Wc = ri.Wr = ri.Wm = 1;
+      rl = ResidentLaunch{};
+      rl.ninst = 1;
+      rl.cluster = K;
+      rl.warps_per_cta = wpc;
+      rl.stage_elems = (uint32_t)stage;
+      rl.meta_smem = (uint32_t)with_meta;
+      rl.group = 3;
+      rl.smem_bytes = smem < 1024 ? 1024 : smem;
+      return true;
+    }
+  return false;
+}
+
 // Geometry of the resident kernel for cluster size K; false if it does not fit.
 // mode (ResidentLaunch::group) 0: tiles processed by single warps (k_resident),
 // one stage per warp; 1: by four-warp groups (k_resident_group), one stage per
@@ -218,6 +253,7 @@ static uint32_t choose_lines(uint64_t lines, uint64_t nwarps, uint64_t entries) 
 // single warps, one stage per warp (a group uses its four warps' stages).
 static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K, ResidentLaunch& rl,
                           ResidentInstance& ri, uint32_t mode = 0) {
+  if (mode == 3) return plan_resident_lean(pr, st, K, rl, ri);
   const bool group = mode == 1;
   const HostProgram& hp = pr->hp;
   const size_t esz = st->esz;
@@ -308,7 +344,10 @@ static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, u
 
 // ResidentLaunch::group of a resident strategy.
 static uint32_t resident_mode(uint32_t strategy) {
-  return strategy == QPE_STRATEGY_GROUP ? 1u : (strategy == QPE_STRATEGY_HYBRID ? 2u : 0u);
+  if (strategy == QPE_STRATEGY_GROUP) return 1u;
+  if (strategy == QPE_STRATEGY_HYBRID) return 2u;
+  if (strategy == QPE_STRATEGY_LEAN) return 3u;
+  return 0u;
 }
 
 // Strategy for (program, state): explicit, or timed on one power per candidate.
@@ -322,7 +361,8 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     K = 1;
     return;
   }
-  if (strategy == QPE_STRATEGY_CLUSTER || strategy == QPE_STRATEGY_GROUP || strategy == QPE_STRATEGY_HYBRID) {
+  if (strategy == QPE_STRATEGY_CLUSTER || strategy == QPE_STRATEGY_GROUP || strategy == QPE_STRATEGY_HYBRID ||
+      strategy == QPE_STRATEGY_LEAN) {
     const uint32_t mode = resident_mode(strategy);
     if (K == 0) {
       for (uint32_t c = mode ? 1 : 2; c <= 16 && !K; c *= 2)
@@ -353,6 +393,7 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     if (plan_resident(pr, st, c, rl, ri)) cands.push_back({c == 1 ? QPE_STRATEGY_RESIDENT : QPE_STRATEGY_CLUSTER, c});
     if (plan_resident(pr, st, c, rl, ri, 1)) cands.push_back({QPE_STRATEGY_GROUP, c});
     if (plan_resident(pr, st, c, rl, ri, 2)) cands.push_back({QPE_STRATEGY_HYBRID, c});
+    if (plan_resident(pr, st, c, rl, ri, 3)) cands.push_back({QPE_STRATEGY_LEAN, c});
   }
   cands.push_back({QPE_STRATEGY_TILED, 0});
   if (cands.size() == 1) {
@@ -891,7 +932,7 @@ int qpe_evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts
   return guard([&] {
     check_state(st);
     if (!pr) throw Error(QPE_ERR_INVALID, "null program");
-    if (opts && opts->strategy > QPE_STRATEGY_HYBRID) throw Error(QPE_ERR_INVALID, "unknown strategy");
+    if (opts && opts->strategy > QPE_STRATEGY_LEAN) throw Error(QPE_ERR_INVALID, "unknown strategy");
     if (opts && opts->cluster_size && (opts->cluster_size > 16 || (opts->cluster_size & (opts->cluster_size - 1))))
       throw Error(QPE_ERR_INVALID, "cluster_size must be a power of two <= 16");
     if (opts && (opts->flags & ~(QPE_EVOLVE_FP64_CONTRACT | QPE_EVOLVE_IN_PLACE)))

@@ -163,7 +163,6 @@ __device__ __forceinline__ void group_mix_ops(const DevOp* __restrict__ ops, con
   const uint32_t q = gt & 3u, slot = gt >> 2, nslots = gthreads >> 2;
   const uint32_t w = slot & ((1u << logW) - 1);
   const uint32_t j0 = slot >> logW, jstep = nslots >> logW;
-  const uint32_t jshift = __ffs(jstep) - 1;  // jstep is a power of two
   const uint32_t wj0 = ((gt & ~31u) >> 2) >> logW;  // smallest j0 of this thread's warp
   const bool wvalid = w < nvalid;
   const uint32_t my_parb = wvalid ? parb(w) : 0u;
@@ -235,7 +234,7 @@ __device__ __forceinline__ void group_mix_ops(const DevOp* __restrict__ ops, con
     desc(min(i + 1, n - 1), na, nb);
     const uint2 nx = entry(na.x, na.y, j0);
     const uint32_t tab = a.x, count = a.y;
-    const uint32_t ntrips = (count + jstep - 1) >> jshift;
+    const uint32_t ntrips = (count + jstep - 1) / jstep;
     if (a.w == OP_INLINE) {
       const R c = (R)__hiloint2double((int)b.y, (int)b.x), t = (R)__hiloint2double((int)b.w, (int)b.z);
       const R tn = neg(t);
@@ -288,6 +287,169 @@ __device__ __forceinline__ void group_mix_ops(const DevOp* __restrict__ ops, con
     a = na;
     b = nb;
     x = nx;
+  }
+}
+
+
+// The terms of a row or column pass on one line (a tile of W = 1) by a group,
+// in the form of group_mix_ops: a pair update split over a quad (lane q writes
+// component q of the pair, the partner component from lane q ^ 3), a diagonal
+// update over a lane pair. For a diagonal coefficient (c0, c1) the two results
+// of cmul (tile_ops.cuh: v.x c0 - v.y c1, v.x c1 + v.y c0) are
+//   h0: v.x c0 + v.y (-c1)      h1: v.y c0 + v.x c1
+// bit for bit, so lane h reads its own component, takes the other from lane
+// h ^ 1 and does two multiplications and one addition, like a quad lane.
+//
+// A term whose conditions (occupied orbitals of the line's own string) fail is
+// skipped by the whole group: the tile is one line. Terms with one update per
+// lane (at most gthreads / 4 pairs or gthreads / 2 diagonal entries) and an
+// inline matrix are set up kLineChunk at a time ahead of their updates; a term
+// with more entries runs its trips one after another, and a general pair matrix
+// takes group_ops' general quad update.
+constexpr uint32_t kLineChunk = 4;
+
+template <typename R, class A, bool G, class Elem, class Bar>
+__device__ __forceinline__ void group_line_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
+                                               const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1,
+                                               bool rev, uint32_t L, uint32_t lstr, uint32_t gt, uint32_t gthreads,
+                                               Elem elem, Bar gbar, typename Cx<R>::T* scratch) {
+  using C2 = typename Cx<R>::T;
+  const uint32_t n = op1 - op0;
+  if (n == 0) return;
+  const uint32_t q = gt & 3u, pslot = gt >> 2, pstep = gthreads >> 2;  // pair updates: quads
+  const uint32_t h = gt & 1u, dslot = gt >> 1, dstep = gthreads >> 1;  // diagonal updates: lane pairs
+  const uint32_t wp0 = (gt & ~31u) >> 2, wd0 = (gt & ~31u) >> 1;       // this warp's smallest slots
+  const bool side1 = q >= 2;
+  const uint32_t comp1 = q & 1u, sflip = comp1 ^ 1u;
+  R* const scr = reinterpret_cast<R*>(scratch);
+  auto desc = [&](uint32_t i, uint4& a, uint4& b) {
+    const uint4* src = reinterpret_cast<const uint4*>(ops + (rev ? op1 - 1 - i : op0 + i));
+    a = ldm<G>(src);
+    b = ldm<G>(src + 1);
+  };
+  auto cond = [&](uint32_t z) {  // z = kind | ncond << 8 | cb0 << 16 | cb1 << 24
+    const uint32_t nc = (z >> 8) & 0xffu;
+    uint32_t m = 0;
+    if (nc > 0) m |= 1u << ((z >> 16) & 0xffu);
+    if (nc > 1) m |= 1u << (z >> 24);
+    return (lstr & m) == m;
+  };
+  // One update item of this lane: its own component, the coefficient pair and
+  // the shuffle distance to the lane holding the other operand.
+  struct Item {
+    R* dp;
+    R c, s;
+    uint32_t xd;
+    bool wact;
+  };
+  // Item of trip `tr` of an inline term (a, b) with `count` entries.
+  auto make_item = [&](const uint4& a, const uint4& b, uint32_t count, uint32_t tr) {
+    Item it;
+    const uint32_t kind = a.z & 0xffu;
+    it.c = (R)__hiloint2double((int)b.y, (int)b.x);
+    const R c1 = (R)__hiloint2double((int)b.w, (int)b.z);
+    if (kind == OPK_PAIR) {
+      const uint32_t j = pslot + tr * pstep;
+      const bool act = j < count;
+      const uint2 x = ldm<G>(reinterpret_cast<const uint2*>(pool + a.x) + min(j, count - 1));
+      it.s = (((x.x >> 31) ^ sflip) && act) ? neg(c1) : c1;
+      R* lp = reinterpret_cast<R*>(&elem(x.x & 0x7fffffffu));
+      R* rp = reinterpret_cast<R*>(&elem(x.y));
+      it.dp = act ? (side1 ? rp : lp) + comp1 : scr + comp1;
+      it.xd = 3;
+      it.wact = wp0 + tr * pstep < count;
+    } else {
+      const uint32_t j = dslot + tr * dstep;
+      const bool act = j < count;
+      const uint32_t e = kind == OPK_DIAG_LIST ? ldm<G>(pool + a.x + min(j, count - 1)) : min(j, count - 1);
+      it.s = h ? c1 : neg(c1);
+      it.dp = act ? reinterpret_cast<R*>(&elem(e)) + h : scr + h;
+      it.xd = 1;
+      it.wact = wd0 + tr * dstep < count;
+    }
+    return it;
+  };
+  auto run_item = [&](const Item& it) {
+    if (it.wact) {
+      const R x1 = *it.dp;
+      const R x2 = __shfl_xor_sync(0xffffffffu, x1, it.xd);
+      *it.dp = A::add(A::mul(x1, it.c), A::mul(x2, it.s));
+    }
+  };
+  uint32_t i = 0;
+  while (i < n) {
+    // Set up the next run of up to kLineChunk terms that are skipped or have one
+    // inline update per lane; stop before the first other term.
+    Item its[kLineChunk];
+    bool has[kLineChunk];
+    uint32_t m = 0;
+    bool stop = false;
+#pragma unroll
+    for (uint32_t k = 0; k < kLineChunk; ++k) {
+      has[k] = false;
+      its[k] = Item{scr, (R)0, (R)0, 1u, false};
+      if (!stop && i + k < n) {
+        uint4 a, b;
+        desc(i + k, a, b);
+        const uint32_t kind = a.z & 0xffu;
+        const uint32_t count = kind == OPK_DIAG_ALL ? L : a.y;
+        if (!cond(a.z) || count == 0) {
+          m = k + 1;  // skipped by the whole group: no update, no barrier
+        } else if (a.w == OP_INLINE && count <= (kind == OPK_PAIR ? pstep : dstep)) {
+          its[k] = make_item(a, b, count, 0);
+          has[k] = true;
+          m = k + 1;
+        } else {
+          stop = true;
+        }
+      }
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kLineChunk; ++k) {
+      if (has[k]) {
+        run_item(its[k]);
+        gbar();
+      }
+    }
+    i += m;
+    if (stop) {
+      // term i: several trips, or a general pair matrix
+      uint4 a, b;
+      desc(i, a, b);
+      const uint32_t kind = a.z & 0xffu;
+      const uint32_t count = kind == OPK_DIAG_ALL ? L : a.y;
+      if (a.w == OP_INLINE) {
+        const uint32_t ntrips = (count + (kind == OPK_PAIR ? pstep : dstep) - 1) / (kind == OPK_PAIR ? pstep : dstep);
+        for (uint32_t tr = 0; tr < ntrips; ++tr) run_item(make_item(a, b, count, tr));
+      } else {
+        const double2* cr = reinterpret_cast<const double2*>(coef + 8 * (size_t)a.w);
+        const double2 e0 = __ldg(cr), e1 = __ldg(cr + 1), o0 = __ldg(cr + 2), o1 = __ldg(cr + 3);
+        for (uint32_t j = pslot; j < count + (pstep - 1) - ((count + pstep - 1) % pstep); j += pstep) {
+          R out = (R)0;
+          R* dst = nullptr;
+          if (j < count) {
+            const uint2 x = ldm<G>(reinterpret_cast<const uint2*>(pool + a.x) + j);
+            R* lp = reinterpret_cast<R*>(&elem(x.x & 0x7fffffffu));
+            R* rp = reinterpret_cast<R*>(&elem(x.y));
+            const uint32_t par = x.x >> 31;
+            const C2 vl = *reinterpret_cast<const C2*>(lp), vr = *reinterpret_cast<const C2*>(rp);
+            const R m0r = (R)(par ? o0.x : e0.x), m0i = (R)(par ? o0.y : e0.y);
+            const R m1r = (R)(par ? o1.x : e1.x), m1i = (R)(par ? o1.y : e1.y);
+            const R ma_r = q < 2 ? m0r : m1r, ma_i = q < 2 ? m0i : m1i;  // multiplies l
+            const R mb_r = q < 2 ? m1r : m0r, mb_i = q < 2 ? m1i : m0i;  // multiplies r
+            const bool im = q & 1;
+            const R g1 = im ? ma_i : ma_r, g2 = im ? ma_r : neg(ma_i);
+            const R g3 = im ? mb_i : mb_r, g4 = im ? mb_r : neg(mb_i);
+            out = A::add(A::add(A::mul(vl.x, g1), A::mul(vl.y, g2)), A::add(A::mul(vr.x, g3), A::mul(vr.y, g4)));
+            dst = (q >= 2 ? rp : lp) + (q & 1);
+          }
+          __syncwarp();
+          if (dst) *dst = out;
+        }
+      }
+      gbar();
+      ++i;
+    }
   }
 }
 

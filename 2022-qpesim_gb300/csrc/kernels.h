@@ -96,6 +96,8 @@ struct ResidentLaunch {
                                   // 2: column-pair passes by four-warp groups (whose
                                   //    stage is their four warps' stages), row and
                                   //    column passes by single warps (k_resident)
+                                  // 3: every tile by a three-warp group (k_resident_lean);
+                                  //    stage_elems is per group
   uint32_t meta_smem;             // 1: term descriptors, index pool, passes and line
                                   //    strings are staged in every CTA's shared memory
   size_t smem_bytes;

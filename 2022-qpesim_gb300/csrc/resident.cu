@@ -452,6 +452,156 @@ __global__ void __launch_bounds__(512) k_resident_group(const ResidentInstance* 
   }
 }
 
+// Every tile processed by a group of three warps with the lean runners
+// (group_ops.cuh): one column, one row or one column pair per group tile, pair
+// updates split over quads and diagonal updates over lane pairs, the partner
+// operand by shuffle. Three-warp groups give a cluster of 16 CTAs of 15 warps
+// 80 groups, more than the 70 columns of an n = 16 block, so that the long
+// first column pass runs one column per group; a term of up to 24 pairs or 48
+// diagonal entries is one update per lane. Tiles go round-robin over the
+// cluster's groups; rows are processed by the CTA that owns them.
+constexpr uint32_t kLeanWarps = 3;
+
+template <typename R, class A, bool MS>
+__global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* __restrict__ insts,
+                                                       uint32_t stage_elems) {
+  using C2 = typename Cx<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ C2 scratch_s[16 / kLeanWarps];  // per group: target of the lanes without an update
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t K = cl.num_blocks();
+  const uint32_t rank = cl.block_rank();
+  const ResidentInstance I = insts[blockIdx.x / K];
+  const uint32_t wpc = blockDim.x >> 5;
+  const uint32_t gthreads = 32 * kLeanWarps, ngrp = wpc / kLeanWarps;
+  const uint32_t grp = threadIdx.x / gthreads, gt = threadIdx.x - grp * gthreads;
+  const uint32_t Ca = I.Ca, Cb = I.Cb, Rk = I.rows_per_cta;
+  const uint32_t row0 = min(rank * Rk, Ca), row1 = min(row0 + Rk, Ca);
+  C2* blk = reinterpret_cast<C2*>(smem_raw);
+  C2* stage = blk + (size_t)Rk * Cb + (size_t)grp * stage_elems;
+  C2* __restrict__ gstate = reinterpret_cast<C2*>(I.state);
+  C2* scratch = scratch_s + grp;
+  const uint64_t ld = (uint64_t)Ca * Cb;
+  const uint32_t nown = (row1 - row0) * Cb;
+
+  auto barrier = [&]() {
+    if (K == 1) __syncthreads();
+    else cl.sync();
+  };
+  auto gbar = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(gthreads) : "memory"); };
+  auto at = [&](uint32_t a, uint32_t b) -> C2* {
+    const uint32_t r = a / Rk;
+    return cta_ptr(blk, r, K) + (size_t)(a - r * Rk) * Cb + b;
+  };
+
+  const DevOp* ops = I.ops;
+  const uint32_t* pool = I.pool;
+  const Pass* passes = I.passes;
+  const uint32_t* strA = I.strA;
+  const uint32_t* strB = I.strB;
+  if constexpr (MS) {
+    const size_t head = ((size_t)Rk * Cb + (size_t)ngrp * stage_elems) * sizeof(C2);
+    unsigned char* meta = smem_raw + ((head + 15) & ~(size_t)15);
+    DevOp* ops_s = reinterpret_cast<DevOp*>(meta);
+    uint32_t* pool_s = reinterpret_cast<uint32_t*>(meta + (size_t)I.nops * sizeof(DevOp));
+    Pass* passes_s = reinterpret_cast<Pass*>(pool_s + ((I.pool_words + 3u) & ~3u));
+    uint32_t* strA_s = reinterpret_cast<uint32_t*>(passes_s + I.npasses);
+    uint32_t* strB_s = strA_s + Ca;
+    const uint4* osrc = reinterpret_cast<const uint4*>(I.ops);
+    for (uint32_t i = threadIdx.x; i < I.nops * 2; i += blockDim.x) reinterpret_cast<uint4*>(ops_s)[i] = osrc[i];
+    for (uint32_t i = threadIdx.x; i < I.pool_words; i += blockDim.x) pool_s[i] = I.pool[i];
+    const uint32_t* psrc = reinterpret_cast<const uint32_t*>(I.passes);
+    for (uint32_t i = threadIdx.x; i < I.npasses * (uint32_t)(sizeof(Pass) / 4); i += blockDim.x)
+      reinterpret_cast<uint32_t*>(passes_s)[i] = psrc[i];
+    for (uint32_t i = threadIdx.x; i < Ca; i += blockDim.x) strA_s[i] = I.strA[i];
+    for (uint32_t i = threadIdx.x; i < Cb; i += blockDim.x) strB_s[i] = I.strB[i];
+    ops = ops_s;
+    pool = pool_s;
+    passes = passes_s;
+    strA = strA_s;
+    strB = strB_s;
+  }
+  constexpr bool G = !MS;
+  constexpr int kDepth = sizeof(R) == 8 ? 2 : 4;
+  const bool in_group = grp < ngrp;  // threads past the last whole group only join the CTA barriers
+
+  {
+    const C2* src = gstate + (uint64_t)(I.in_place ? I.first : I.first - 1) * ld + (uint64_t)row0 * Cb;
+    for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) blk[i] = src[i];
+  }
+  barrier();
+
+  const uint32_t nsweeps = I.steps * I.order;
+  for (uint32_t k = I.first; k < I.last; ++k) {
+    for (uint32_t sw = 0; sw < nsweeps; ++sw) {
+      const bool rev = I.order == 2 && (sw & 1);
+      for (uint32_t pj = 0; pj < I.npasses; ++pj) {
+        const uint32_t pi = rev ? I.npasses - 1 - pj : pj;
+        const Pass P = passes[pi];
+        if (!in_group) {
+          // no tile
+        } else if (P.type == PASS_ROW) {
+          // this CTA's rows, one per group tile, in place
+          for (uint32_t r = row0 + grp; r < row1; r += ngrp) {
+            C2* line = blk + (size_t)(r - row0) * Cb;
+            group_line_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Cb, ldm<G>(strA + r), gt, gthreads,
+                                    [&](uint32_t e) -> C2& { return line[e]; }, gbar, scratch);
+          }
+        } else if (P.type == PASS_COL) {
+          for (uint32_t b = grp * K + rank; b < Cb; b += K * ngrp) {
+            const uint32_t lstr = ldm<G>(strB + b);
+            if (K == 1) {
+              group_line_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, lstr, gt, gthreads,
+                                      [&](uint32_t e) -> C2& { return blk[(size_t)e * Cb + b]; }, gbar, scratch);
+            } else {
+              auto ok = [](uint32_t) { return true; };
+              auto remote = [&](uint32_t i) { return at(i, b); };
+              auto local = [&](uint32_t i) { return stage + i; };
+              group_copy<C2, kDepth>(Ca, gt, gthreads, ok, remote, local);
+              gbar();
+              group_line_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, lstr, gt, gthreads,
+                                      [&](uint32_t e) -> C2& { return stage[e]; }, gbar, scratch);
+              group_copy<C2, kDepth>(Ca, gt, gthreads, ok, local, remote);
+              gbar();
+            }
+          }
+        } else {  // PASS_MIX: one column pair per group tile
+          const uint2* __restrict__ mt = reinterpret_cast<const uint2*>(pool + P.mixtab);
+          for (uint32_t tile = grp * K + rank; tile < P.mixcount; tile += K * ngrp) {
+            const uint2 pr = ldm<G>(mt + tile);
+            const uint32_t b01 = pr.x & 0x7fffffffu, b10 = pr.y, pb = pr.x >> 31;
+            auto parb = [&](uint32_t) { return pb; };
+            if (K == 1) {
+              auto left = [&](uint32_t, uint32_t a) -> C2& { return blk[(size_t)a * Cb + b01]; };
+              auto right = [&](uint32_t, uint32_t a) -> C2& { return blk[(size_t)a * Cb + b10]; };
+              group_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, 0, 1, gt, gthreads, left, right, parb,
+                                     gbar, scratch);
+            } else {
+              // element i: row i >> 1, side i & 1 (gthreads is even: a thread's side is fixed)
+              const uint32_t mycol = (gt & 1) ? b10 : b01;
+              auto ok = [](uint32_t) { return true; };
+              auto remote = [&](uint32_t i) { return at(i >> 1, mycol); };
+              auto local = [&](uint32_t i) { return stage + i; };
+              group_copy<C2, kDepth>(Ca << 1, gt, gthreads, ok, remote, local);
+              gbar();
+              auto left = [&](uint32_t, uint32_t a) -> C2& { return stage[2 * a]; };
+              auto right = [&](uint32_t, uint32_t a) -> C2& { return stage[2 * a + 1]; };
+              group_mix_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, 0, 1, gt, gthreads, left, right, parb,
+                                     gbar, scratch);
+              group_copy<C2, kDepth>(Ca << 1, gt, gthreads, ok, local, remote);
+              gbar();
+            }
+          }
+        }
+        barrier();
+      }
+    }
+    C2* dst = gstate + (uint64_t)(I.in_place ? I.first : k) * ld + (uint64_t)row0 * Cb;
+    for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) dst[i] = blk[i];
+    barrier();
+  }
+}
+
 template <typename R, class A, bool MS>
 static cudaError_t launch_res(const ResidentLaunch& rl, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
@@ -467,7 +617,8 @@ static cudaError_t launch_res(const ResidentLaunch& rl, cudaStream_t s) {
   cfg.attrs = at;
   cfg.numAttrs = 1;
   auto kern = rl.group == 1 ? k_resident_group<R, A, MS>
-                            : (rl.group == 2 ? k_resident<R, A, MS, true> : k_resident<R, A, MS, false>);
+                            : (rl.group == 2 ? k_resident<R, A, MS, true>
+                                             : (rl.group == 3 ? k_resident_lean<R, A, MS> : k_resident<R, A, MS, false>));
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rl.smem_bytes);
   if (e) return e;
   if (rl.cluster > 8) {
@@ -496,6 +647,8 @@ static cudaError_t carveout_t(int percent) {
   cudaError_t e = cudaFuncSetAttribute(k_resident<R, A, MS, false>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
   if (e) return e;
   e = cudaFuncSetAttribute(k_resident<R, A, MS, true>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+  if (e) return e;
+  e = cudaFuncSetAttribute(k_resident_lean<R, A, MS>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
   if (e) return e;
   return cudaFuncSetAttribute(k_resident_group<R, A, MS>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
 }

@@ -145,7 +145,9 @@ class DeviceState:
         global-memory tile passes, 4 a cluster whose tiles are processed by
         four-warp groups with every update split over four lanes, 5 a cluster
         whose column-pair tiles are processed as in 4 and row and column tiles
-        as in 2. fp64_contract allows FMAs in complex128 (within 1e-12 of the
+        as in 2, 6 a cluster whose rows, columns and column pairs are each
+        processed by a three-warp group (pair updates over four lanes, diagonal
+        updates over two). fp64_contract allows FMAs in complex128 (within 1e-12 of the
         reference instead of bit-identical)."""
         opts = N.EvolveOpts(strategy, first_power, last_power, cluster_size,
                             N.QPE_EVOLVE_FP64_CONTRACT if fp64_contract else 0, 0)
@@ -169,7 +171,7 @@ class DeviceState:
 
     def last_strategy(self) -> tuple:
         """(strategy, cluster size) of the last evolve: 1 resident, 2 cluster, 3 tiled, 4 grouped cluster,
-        5 cluster with grouped column-pair tiles."""
+        5 cluster with grouped column-pair tiles, 6 cluster of three-warp groups."""
         s, k = C.c_uint32(), C.c_uint32()
         N.check(self._lib.qpe_state_last_strategy(self._h, C.byref(s), C.byref(k)))
         return s.value, k.value

@@ -302,12 +302,14 @@ def run_ours(args, w, rank, ws, local):
         kernel = "k_pass (evolution tile passes, one launch per pass)"
         launches = args.steps * (npow * (info["num_passes_per_power"] + 2) + 1 + 2 + 1)
     else:
-        kernel = (f"{'k_resident_group' if strat == 4 else 'k_resident'} (whole evolution in one launch, "
+        kname = {4: "k_resident_group", 6: "k_resident_lean"}.get(strat, "k_resident")
+        kernel = (f"{kname} (whole evolution in one launch, "
                   f"cluster of {kc} CTA(s){', column pairs by four-warp groups' if strat == 5 else ''})")
         launches = args.steps * (1 + 2)
     strategy_name = {1: "resident (one CTA)", 2: f"cluster of {kc} CTAs", 3: "tiled passes",
                      4: f"cluster of {kc} CTAs, four-warp tile groups",
-                     5: f"cluster of {kc} CTAs, column-pair tiles by four-warp groups"}.get(strat, "?")
+                     5: f"cluster of {kc} CTAs, column-pair tiles by four-warp groups",
+                     6: f"cluster of {kc} CTAs, every tile by a three-warp group"}.get(strat, "?")
     line = {
         "metric": "amplitude-term updates/s per Trotter step",
         "value": value,
@@ -749,7 +751,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--strategy", type=int, default=0,
                     help="0 auto, 1 one-CTA resident, 2 cluster, 3 tiled, 4 cluster with four-warp groups, "
-                         "5 cluster with column pairs by four-warp groups")
+                         "5 cluster with column pairs by four-warp groups, 6 cluster of three-warp groups")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per cluster for --strategy 2 (0: smallest)")
     ap.add_argument("--powers", type=int, default=0,
                     help="evolve only the first K controlled powers (profiling runs; not a workload's figure)")

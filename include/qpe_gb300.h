@@ -210,6 +210,9 @@ int qpe_state_zero(qpe_state* st);
                                    groups with every update split over four lanes */
 #define QPE_STRATEGY_HYBRID 5   /* as CLUSTER (cluster_size 1..16): column-pair passes as GROUP,
                                    row and column passes as CLUSTER */
+#define QPE_STRATEGY_LEAN 6     /* as CLUSTER (cluster_size 1..16): every row, column or column
+                                   pair processed by a three-warp group, pair updates split over
+                                   four lanes and diagonal updates over two */
 
 /* complex128 only: allow fused multiply-adds. Results then differ from the
  * reference's rounding by a few ulps per update (within 1e-12 of it) instead of

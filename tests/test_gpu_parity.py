@@ -222,7 +222,8 @@ def test_pp_fixture_phase_on_gpu(gpu):
 
 @pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 2), (2, 4), (2, 8), (2, 16), (3, 0), (0, 0),
                                               (4, 1), (4, 2), (4, 4), (4, 8), (4, 16),
-                                              (5, 1), (5, 2), (5, 4), (5, 8), (5, 16)])
+                                              (5, 1), (5, 2), (5, 4), (5, 8), (5, 16),
+                                              (6, 1), (6, 2), (6, 4), (6, 8), (6, 16)])
 @pytest.mark.parametrize("n,na,nb,P", [(12, 3, 3, 3), (14, 4, 3, 2), (8, 2, 2, 4), (16, 4, 4, 2)])
 def test_strategies_bit_identical(gpu, orc, strategy, cluster, n, na, nb, P):
     """Every evolution strategy (one CTA resident in shared memory, clusters of 2
@@ -244,7 +245,7 @@ def test_strategies_bit_identical(gpu, orc, strategy, cluster, n, na, nb, P):
     assert np.array_equal(st.download(), ref)
 
 
-@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0), (4, 1), (4, 4), (5, 1), (5, 4)])
+@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0), (4, 1), (4, 4), (5, 1), (5, 4), (6, 1), (6, 4)])
 def test_strategies_complex64(gpu, orc, strategy, cluster):
     q = gpu
     n, N, P = 12, 6, 4
@@ -261,7 +262,7 @@ def test_strategies_complex64(gpu, orc, strategy, cluster):
     assert np.abs(st.download() - ref).max() < 2e-5
 
 
-@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0), (4, 1), (4, 4), (5, 4)])
+@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0), (4, 1), (4, 4), (5, 4), (6, 4)])
 def test_fp64_contract_within_tolerance(gpu, orc, strategy, cluster):
     """With FMAs allowed (QPE_EVOLVE_FP64_CONTRACT) complex128 stays within 1e-12
     of the reference's rounding (here over 15 powers of a 2nd-order, 2-step
@@ -326,7 +327,7 @@ def test_batch_matches_oracle_per_instance(gpu, orc, dtype):
 
 
 @pytest.mark.parametrize("name", sorted(p.name for p in GOLDEN.glob("iqpe_*.npz")))
-@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 2), (3, 0), (0, 0), (4, 2), (5, 2)])
+@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 2), (3, 0), (0, 0), (4, 2), (5, 2), (6, 2)])
 def test_iqpe_golden(gpu, name, strategy, cluster):
     """time_evolve_iqpe (cpp/time_evolution_over_terms.hpp:141-155): block 1 in
     place, applyUnitary's term order, against the reference's own output, through
@@ -362,7 +363,7 @@ def test_iqpe_bit_identical_to_oracle(gpu, orc, strategy):
     assert np.array_equal(st.download(), reg)
 
 
-@pytest.mark.parametrize("strategy,order,steps", [(1, 1, 1), (2, 2, 2), (3, 2, 1), (4, 2, 2), (5, 2, 2)])
+@pytest.mark.parametrize("strategy,order,steps", [(1, 1, 1), (2, 2, 2), (3, 2, 1), (4, 2, 2), (5, 2, 2), (6, 2, 2)])
 def test_in_place_repeats_equal_powers(gpu, strategy, order, steps):
     """r in-place applications to block 1 holding block 0 give block r of the
     ordinary controlled-power evolution, bit for bit, in any strategy."""
