@@ -92,9 +92,9 @@ __global__ void k_pass(PassLaunch pl) {
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
     Sync()();
     if (PT == PASS_MIX) {
-      run_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, lane, tpt, true, parb,
-                        [&](uint32_t a) -> C2& { return st[2 * a]; },
-                        [&](uint32_t a) -> C2& { return st[2 * a + 1]; }, icoef, Sync());
+      chunked_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, lane, tpt, true, parb,
+                            [&](uint32_t a) -> C2& { return st[2 * a]; },
+                            [&](uint32_t a) -> C2& { return st[2 * a + 1]; }, icoef, Sync());
     } else {
       // Lane l owns line l % W and walks entries l / W, l / W + 32 / W, ...
       const uint32_t w = lane & (W - 1);

@@ -267,6 +267,102 @@ __device__ __forceinline__ void run_mix_ops(const DevOp* __restrict__ ops, const
   }
 }
 
+// The terms of a column-pair tile in chunks (one tile per CTA or per warp, one
+// pair update per thread and trip): the descriptors, coefficients, table
+// entries and element addresses of kPairChunk terms, kPairTrips trips each, are
+// loaded and computed before the chunk's first update, so that a term costs its
+// shared-memory loads, arithmetic, stores and barrier, not a chain of dependent
+// global loads. Only inline pair matrices take this form (every term of the
+// reference's getters); a chunk with another term, or with more entries than
+// kPairTrips trips cover, runs through run_mix_ops. The update is pair_update's
+// reduced form, bit for bit.
+constexpr uint32_t kPairChunk = 4;
+constexpr uint32_t kPairTrips = 3;
+
+template <typename R, class A, class Left, class Right, class Sync>
+__device__ __forceinline__ void chunked_mix_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
+                                                const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1,
+                                                bool rev, uint32_t jl, uint32_t jstep, bool active, uint32_t parb,
+                                                Left left, Right right, const double2* __restrict__ icoef, Sync sync) {
+  using C2 = typename Cx<R>::T;
+  const uint32_t n = op1 - op0;
+  // The terms of a MIX pass share one table length (pairs of alpha strings for
+  // one excitation): passes whose tables need more trips skip the chunked form.
+  if (n == 0) return;
+  if (__ldg(reinterpret_cast<const uint4*>(ops + op0)).y > kPairTrips * jstep) {
+    run_mix_ops<R, A, true>(ops, coef, pool, op0, op1, rev, jl, jstep, active, parb, left, right, icoef, sync);
+    return;
+  }
+  for (uint32_t i0 = 0; i0 < n; i0 += kPairChunk) {
+    const uint32_t m = min(kPairChunk, n - i0);
+    R cc[kPairChunk], tt[kPairChunk];
+    C2* lp[kPairChunk][kPairTrips];
+    C2* rp[kPairChunk][kPairTrips];
+    uint32_t par[kPairChunk];  // bit tr: parity of trip tr
+    uint32_t okm[kPairChunk];  // bit tr: trip tr has an entry
+    bool fast = true;
+#pragma unroll
+    for (uint32_t k = 0; k < kPairChunk; ++k) {
+      cc[k] = tt[k] = (R)0;
+      par[k] = okm[k] = 0;
+#pragma unroll
+      for (uint32_t tr = 0; tr < kPairTrips; ++tr) lp[k][tr] = rp[k][tr] = nullptr;
+      if (k < m) {
+        const uint32_t o = rev ? op1 - 1 - (i0 + k) : op0 + i0 + k;
+        const uint4* src = reinterpret_cast<const uint4*>(ops + o);
+        const uint4 a = __ldg(src), b = __ldg(src + 1);
+        fast = fast && a.w == OP_INLINE && (a.z & 0xffu) == (uint32_t)OPK_PAIR && a.y <= kPairTrips * jstep;
+        double c0 = __hiloint2double((int)b.y, (int)b.x), c1 = __hiloint2double((int)b.w, (int)b.z);
+        if (icoef) {
+          const double2 ic = __ldg(icoef + o);
+          c0 = ic.x;
+          c1 = ic.y;
+        }
+        cc[k] = (R)c0;
+        tt[k] = (R)c1;
+#pragma unroll
+        for (uint32_t tr = 0; tr < kPairTrips; ++tr) {
+          const uint32_t j = jl + tr * jstep;
+          if (active && j < a.y) {
+            const uint2 x = __ldg(reinterpret_cast<const uint2*>(pool + a.x) + j);
+            lp[k][tr] = &left(x.x & 0x7fffffffu);
+            rp[k][tr] = &right(x.y);
+            par[k] |= (((x.x >> 31) ^ parb) & 1u) << tr;
+            okm[k] |= 1u << tr;
+          }
+        }
+      }
+    }
+    if (!fast) {
+      run_mix_ops<R, A, true>(ops, coef, pool, rev ? op1 - (i0 + m) : op0 + i0, rev ? op1 - i0 : op0 + i0 + m, rev,
+                              jl, jstep, active, parb, left, right, icoef, sync);
+      continue;
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kPairChunk; ++k) {
+      if (k < m) {
+#pragma unroll
+        for (uint32_t tr = 0; tr < kPairTrips; ++tr) {
+          if ((okm[k] >> tr) & 1u) {
+            C2& l = *lp[k][tr];
+            C2& r = *rp[k][tr];
+            const C2 vl = l, vr = r;
+            const R c = cc[k], t = ((par[k] >> tr) & 1u) ? neg(tt[k]) : tt[k];
+            C2 nl, nr;
+            nl.x = A::sub(A::mul(vl.x, c), A::mul(vr.y, t));
+            nl.y = A::add(A::mul(vl.y, c), A::mul(vr.x, t));
+            nr.x = A::sub(A::mul(vr.x, c), A::mul(vl.y, t));
+            nr.y = A::add(A::mul(vl.x, t), A::mul(vr.y, c));
+            l = nl;
+            r = nr;
+          }
+        }
+        sync();
+      }
+    }
+  }
+}
+
 }  // namespace qpe
 
 #endif  // QPE_TILE_OPS_CUH_
