@@ -101,8 +101,9 @@ __global__ void k_pass(PassLaunch pl) {
       const bool active = w < nl;
       const uint32_t line = (PT == PASS_COL) ? b0 + w : row;
       const uint32_t lstr = active ? __ldg(((PT == PASS_COL) ? pl.strB : pl.strA) + line) : 0u;
-      run_line_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, L, lane >> logW, tpt >> logW,
-                         active, lstr, [&](uint32_t e) -> C2& { return st[(e << logW) + w]; }, icoef, Sync());
+      chunked_line_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, L, lane >> logW,
+                             tpt >> logW, active, lstr, [&](uint32_t e) -> C2& { return st[(e << logW) + w]; }, icoef,
+                             Sync());
     }
     for (uint32_t i = lane; i < nst; i += tpt)
       if ((i & (W - 1)) < nl) blk[goff(i)] = st[i];

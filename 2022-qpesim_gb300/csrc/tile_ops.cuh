@@ -363,6 +363,122 @@ __device__ __forceinline__ void chunked_mix_ops(const DevOp* __restrict__ ops, c
   }
 }
 
+// The terms of a row or column tile (run_line_ops' layout: thread entries jl,
+// jl + jstep, ... of each term on its own line) in chunks, like
+// chunked_mix_ops: the descriptors of kPairChunk terms are loaded first, and
+// when all of them are inline with at most kPairTrips trips, their table entries
+// and element addresses follow before the first update. Pair terms take
+// pair_update's reduced form, diagonal terms diag_update, bit for bit; a line
+// whose string fails a term's conditions skips it. Any other chunk runs through
+// run_line_ops.
+template <typename R, class A, class Elem, class Sync>
+__device__ __forceinline__ void chunked_line_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
+                                                 const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1,
+                                                 bool rev, uint32_t L, uint32_t jl, uint32_t jstep, bool active,
+                                                 uint32_t lstr, Elem elem, const double2* __restrict__ icoef,
+                                                 Sync sync) {
+  using C2 = typename Cx<R>::T;
+  const uint32_t n = op1 - op0;
+  for (uint32_t i0 = 0; i0 < n; i0 += kPairChunk) {
+    const uint32_t m = min(kPairChunk, n - i0);
+    uint4 da[kPairChunk];
+    R cc[kPairChunk], tt[kPairChunk];
+    bool fast = true;
+#pragma unroll
+    for (uint32_t k = 0; k < kPairChunk; ++k) {
+      da[k] = make_uint4(0u, 0u, 0u, 0u);
+      cc[k] = tt[k] = (R)0;
+      if (k < m) {
+        const uint32_t o = rev ? op1 - 1 - (i0 + k) : op0 + i0 + k;
+        const uint4* src = reinterpret_cast<const uint4*>(ops + o);
+        const uint4 a = __ldg(src), b = __ldg(src + 1);
+        const uint32_t kind = a.z & 0xffu;
+        const uint32_t count = kind == OPK_DIAG_ALL ? L : a.y;
+        fast = fast && a.w == OP_INLINE && count <= kPairTrips * jstep;
+        double c0 = __hiloint2double((int)b.y, (int)b.x), c1 = __hiloint2double((int)b.w, (int)b.z);
+        if (icoef) {
+          const double2 ic = __ldg(icoef + o);
+          c0 = ic.x;
+          c1 = ic.y;
+        }
+        da[k] = a;
+        cc[k] = (R)c0;
+        tt[k] = (R)c1;
+      }
+    }
+    if (!fast) {
+      run_line_ops<R, A, true>(ops, coef, pool, rev ? op1 - (i0 + m) : op0 + i0, rev ? op1 - i0 : op0 + i0 + m, rev,
+                               L, jl, jstep, active, lstr, elem, icoef, sync);
+      continue;
+    }
+    C2* p1[kPairChunk][kPairTrips];
+    C2* p2[kPairChunk][kPairTrips];
+    uint32_t par[kPairChunk];  // bit tr: parity of trip tr (pairs)
+    uint32_t okm[kPairChunk];  // bit tr: trip tr has an entry on a line the term acts on
+#pragma unroll
+    for (uint32_t k = 0; k < kPairChunk; ++k) {
+      par[k] = okm[k] = 0;
+#pragma unroll
+      for (uint32_t tr = 0; tr < kPairTrips; ++tr) p1[k][tr] = p2[k][tr] = nullptr;
+      if (k < m) {
+        const uint4 a = da[k];
+        const uint32_t kind = a.z & 0xffu, nc = (a.z >> 8) & 0xffu;
+        uint32_t cm = 0;
+        if (nc > 0) cm |= 1u << ((a.z >> 16) & 0xffu);
+        if (nc > 1) cm |= 1u << (a.z >> 24);
+        const bool on = active && (lstr & cm) == cm;
+        const uint32_t count = kind == OPK_DIAG_ALL ? L : a.y;
+#pragma unroll
+        for (uint32_t tr = 0; tr < kPairTrips; ++tr) {
+          const uint32_t j = jl + tr * jstep;
+          if (on && j < count) {
+            if (kind == OPK_PAIR) {
+              const uint2 x = __ldg(reinterpret_cast<const uint2*>(pool + a.x) + j);
+              p1[k][tr] = &elem(x.x & 0x7fffffffu);
+              p2[k][tr] = &elem(x.y);
+              par[k] |= (x.x >> 31) << tr;
+            } else {
+              p1[k][tr] = &elem(kind == OPK_DIAG_LIST ? __ldg(pool + a.x + j) : j);
+            }
+            okm[k] |= 1u << tr;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kPairChunk; ++k) {
+      if (k < m) {
+        const bool pair = (da[k].z & 0xffu) == OPK_PAIR;
+#pragma unroll
+        for (uint32_t tr = 0; tr < kPairTrips; ++tr) {
+          if ((okm[k] >> tr) & 1u) {
+            if (pair) {
+              C2& l = *p1[k][tr];
+              C2& r = *p2[k][tr];
+              const C2 vl = l, vr = r;
+              const R c = cc[k], t = ((par[k] >> tr) & 1u) ? neg(tt[k]) : tt[k];
+              C2 nl, nr;
+              nl.x = A::sub(A::mul(vl.x, c), A::mul(vr.y, t));
+              nl.y = A::add(A::mul(vl.y, c), A::mul(vr.x, t));
+              nr.x = A::sub(A::mul(vr.x, c), A::mul(vl.y, t));
+              nr.y = A::add(A::mul(vl.x, t), A::mul(vr.y, c));
+              l = nl;
+              r = nr;
+            } else {
+              C2& v = *p1[k][tr];
+              R xr, xi;
+              cmul<A>(v.x, v.y, cc[k], tt[k], xr, xi);
+              v.x = xr;
+              v.y = xi;
+            }
+          }
+        }
+        sync();
+      }
+    }
+  }
+}
+
 }  // namespace qpe
 
 #endif  // QPE_TILE_OPS_CUH_
