@@ -47,7 +47,7 @@ WORKLOADS = {
 }
 # BASELINE configs[3]: the batching form.
 WORKLOADS["batched-256"] = dict(batch=True, count=256, sizes=(12, 14, 16, 18, 20), P=6, dt=0.05, order=1, steps=1,
-                                dtype="c64", seed=2024,
+                                dtype="c64", seed=2024, check_c128=True,
                                 desc="Batching form: 256 seeded Hamiltonians, n uniform in {12,14,16,18,20}, N=n/2 "
                                      "(odd N split ceil/floor over the spins), 6 ancilla qubits, complex64 with FP64 "
                                      "coefficients and histograms, 1st-order Trotter dt=0.05, Hartree-Fock starts, "
@@ -456,6 +456,30 @@ def cpu_baseline_batch(q, w, terms, budget_s=20.0):
     return total_touch / total_t, max(cores.values()), "one instance per size, one at a time: " + "; ".join(parts)
 
 
+def batch_phase_check(q, progs, P, b0, probs64, device):
+    """Every instance's eigenphase from the complex64 batch against a complex128
+    batch of the same programs (the plain FP64 path: bit-identical to the oracle
+    per instance), after the timed steps. Phases are the sub-bin estimates of the
+    histograms, in turns (fractions of 2 pi)."""
+    ref = q.Batch(progs, P, dtype=np.complex128, device=device)
+    for i, a in enumerate(b0):
+        ref.upload(i, a.astype(np.complex128))
+    ref.run()
+    d = []
+    same_bin = 0
+    for i in range(len(progs)):
+        p128 = ref.phase_probs(i)
+        p64 = probs64[i]
+        same_bin += int(np.argmax(p64) == np.argmax(p128))
+        dp = abs(q.subbin_phase(p64) - q.subbin_phase(p128))
+        d.append(min(dp, 1.0 - dp))
+    d = np.array(d)
+    return {"against": "complex128 batch of the same programs on the GPU (the plain FP64 path)",
+            "instances": len(progs), "same_argmax_bin": same_bin,
+            "max_phase_error_turns": float(d.max()), "max_phase_error_rad": float(2 * np.pi * d.max()),
+            "median_phase_error_rad": float(2 * np.pi * np.median(d))}
+
+
 def run_batch(args, w, rank, ws, local):
     q = graft.load_package()
     N = q._native
@@ -552,6 +576,8 @@ def run_batch(args, w, rank, ws, local):
             "touches_per_s_alone": c["touches_per_power"] / (ms / 1e3) if ms > 0 else None,
             "tile": {"lines": c["tile_lines"], "warps_per_cta": c["warps_per_cta"]}}
     line["per_size"] = per_size
+    if w.get("check_c128") and w["dtype"] == "c64":
+        line["precision_check"] = batch_phase_check(q, progs, P, b0, probs, local)
     if rank == 0 and not args.no_cpu_baseline:
         r, cores, sample = cpu_baseline_batch(q, w, terms)
         line["cpu_baseline"] = {"value": r, "unit": "touches/s", "cores": cores, "kind": "port", "sample": sample}
