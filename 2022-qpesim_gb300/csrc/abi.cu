@@ -166,6 +166,14 @@ PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_opt
   const uint64_t entries = binom((int)hp.M - 2, (int)(pass.type == PASS_ROW ? hp.nb : hp.na) - 1) *
                            (pass.type == PASS_COL ? W : 1);
   pl.cta_tile = entries >= 64 ? kCtaTileThreads : 0u;
+  if (pl.cta_tile && pass.type == PASS_COL) {
+    // fewer lines per CTA tile while a thread's entries of a term take more than
+    // the chunked runner's kPairTrips trips
+    const uint64_t e1 = binom((int)hp.M - 2, (int)hp.na - 1);
+    while (W > 1 && e1 * W > (uint64_t)kPairTrips * kCtaTileThreads) W /= 2;
+    pl.W = W;
+    ntiles = (hp.Cb + W - 1) / W;
+  }
   if (pl.cta_tile) {
     wpc = pl.cta_tile / 32;
   } else if (esz == 16) {

@@ -66,6 +66,11 @@ enum OpKind : uint8_t { OPK_PAIR = 0, OPK_DIAG_LIST = 1, OPK_DIAG_ALL = 2 };
 
 enum PassType : uint8_t { PASS_COL = 0, PASS_ROW = 1, PASS_MIX = 2 };
 
+// The chunked term runners of the tile passes (tile_ops.cuh) set up kPairChunk
+// terms at a time, each covering up to kPairTrips entries per thread.
+constexpr uint32_t kPairChunk = 4;
+constexpr uint32_t kPairTrips = 3;
+
 struct Pass {
   uint32_t type;
   uint32_t op0, op1;

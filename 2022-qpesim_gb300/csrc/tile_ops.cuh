@@ -276,8 +276,6 @@ __device__ __forceinline__ void run_mix_ops(const DevOp* __restrict__ ops, const
 // reference's getters); a chunk with another term, or with more entries than
 // kPairTrips trips cover, runs through run_mix_ops. The update is pair_update's
 // reduced form, bit for bit.
-constexpr uint32_t kPairChunk = 4;
-constexpr uint32_t kPairTrips = 3;
 
 template <typename R, class A, class Left, class Right, class Sync>
 __device__ __forceinline__ void chunked_mix_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
