@@ -490,10 +490,10 @@ static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, u
   const HostProgram& hp = pr->hp;
   cudaStream_t s = st->ctx->stream;
   if (!st->work.p) st->work.alloc(st->ld * st->esz);
-  // Working block <- block first - 1 (block first when evolving in place).
-  const size_t src = in_place ? first : first - 1;
-  QPE_CK(cudaMemcpyAsync(st->work.p, st->data.as<char>() + src * st->ld * st->esz, st->ld * st->esz,
-                         cudaMemcpyDeviceToDevice, s));
+  // Working block (stored by columns) <- block first - 1 (block first when
+  // evolving in place).
+  const uint32_t src = in_place ? first : first - 1;
+  QPE_CK(launch_load(st->work.p, st->data.p, (uint32_t)hp.Ca, (uint32_t)hp.Cb, src, st->dtype, s));
   k_set_int<<<1, 1, 0, s>>>(st->dk.as<int>(), (int)first);
   QPE_CK(cudaGetLastError());
   if (st->graph_prog != pr->id || st->graph_exact != (uint32_t)exact || !st->graph) {
@@ -520,7 +520,8 @@ static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, u
     cudaError_t cap_err = cudaSuccess;
     for (const PassLaunch& pl : plans)
       if (cap_err == cudaSuccess) cap_err = launch_pass(pl, st->dtype, s);
-    if (cap_err == cudaSuccess) cap_err = launch_snapshot(st->work.p, st->data.p, st->ld, st->dk.as<int>(), st->dtype, s);
+    if (cap_err == cudaSuccess)
+      cap_err = launch_snapshot(st->work.p, st->data.p, (uint32_t)hp.Ca, (uint32_t)hp.Cb, st->dk.as<int>(), st->dtype, s);
     if (cap_err == cudaSuccess) cap_err = launch_advance(st->dk.as<int>(), s);
     cudaError_t end_err = cudaStreamEndCapture(s, &g);
     if (cap_err != cudaSuccess) {

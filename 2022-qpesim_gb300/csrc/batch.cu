@@ -138,8 +138,8 @@ void tune_class(qpe_batch* b, BatchClass& c) {
       c.wpc = wpc;
       plan_class(b, c);
       QPE_CK(configure_pass_kernels(b->dtype, plans_smem(b, c)));
-      QPE_CK(launch_load_batch(c.works_ptr.as<void*>(), c.states_ptr.as<void*>(), c.ld, 0, (uint32_t)c.members.size(),
-                               b->dtype, s));
+      QPE_CK(launch_load_batch(c.works_ptr.as<void*>(), c.states_ptr.as<void*>(), (uint32_t)c.shape->hp.Ca,
+                               (uint32_t)c.shape->hp.Cb, 0, (uint32_t)c.members.size(), b->dtype, s));
       launch_power(b, c, s);  // warm-up
       QPE_CK(cudaEventRecord(e0, s));
       launch_power(b, c, s);
@@ -184,8 +184,8 @@ void build_graph(qpe_batch* b) {
   try {
     // Working blocks <- block 0; power counter <- 1.
     for (BatchClass& c : b->classes) {
-      QPE_CK(launch_load_batch(c.works_ptr.as<void*>(), c.states_ptr.as<void*>(), c.ld, 0, (uint32_t)c.members.size(),
-                               b->dtype, s));
+      QPE_CK(launch_load_batch(c.works_ptr.as<void*>(), c.states_ptr.as<void*>(), (uint32_t)c.shape->hp.Ca,
+                               (uint32_t)c.shape->hp.Cb, 0, (uint32_t)c.members.size(), b->dtype, s));
       QPE_CK(cudaMemsetAsync(c.dk.p, 0, sizeof(int), s));
       b->launches_per_run += 1;
     }
@@ -213,8 +213,9 @@ void build_graph(qpe_batch* b) {
       QPE_CK(cudaStreamBeginCaptureToGraph(b->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
       QPE_CK(launch_advance(c.dk.as<int>(), b->side));  // k - 1 -> k
       launch_power(b, c, b->side);
-      QPE_CK(launch_snapshot_batch(c.works_ptr.as<void*>(), c.states_ptr.as<void*>(), c.ld, c.dk.as<int>(),
-                                   (uint32_t)c.members.size(), b->dtype, b->side));
+      QPE_CK(launch_snapshot_batch(c.works_ptr.as<void*>(), c.states_ptr.as<void*>(), (uint32_t)c.shape->hp.Ca,
+                                   (uint32_t)c.shape->hp.Cb, c.dk.as<int>(), (uint32_t)c.members.size(), b->dtype,
+                                   b->side));
       QPE_CK(launch_continue_while(c.dk.as<int>(), last, h, b->side));
       cudaGraph_t body_out = nullptr;
       QPE_CK(cudaStreamEndCapture(b->side, &body_out));

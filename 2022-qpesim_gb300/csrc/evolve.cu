@@ -82,9 +82,9 @@ __global__ void k_pass(PassLaunch pl) {
     // a tile pays the L2 latency once rather than once per element.
     auto goff = [&](uint32_t i) -> uint64_t {
       const uint32_t e = i >> logW, w = i & (W - 1);
-      if (PT == PASS_COL) return (uint64_t)e * Cb + b0 + w;
-      if (PT == PASS_ROW) return (uint64_t)row * Cb + e;
-      return (uint64_t)e * Cb + (w ? b10 : b01);
+      if (PT == PASS_COL) return (uint64_t)(b0 + w) * Ca + e;
+      if (PT == PASS_ROW) return (uint64_t)e * Ca + row;
+      return (uint64_t)(w ? b10 : b01) * Ca + e;
     };
     const uint32_t nst = L * W;
     for (uint32_t i = lane; i < nst; i += tpt)
@@ -182,37 +182,60 @@ cudaError_t configure_pass_kernels(int dtype, size_t smem) {
   return e;
 }
 
+// The working block is stored by columns (element (a, b) at b * Ca + a), so that
+// a column, the tile of COL passes and each half of a MIX tile, is contiguous
+// and its gather and scatter are coalesced. The register keeps the reference's
+// row-major blocks (a * Cb + b); loads and snapshots transpose in 32 x 32 tiles
+// through shared memory.
+//
+// dst (C x R, row-major) = transpose of src (R x C, row-major); blockIdx.z picks
+// member z of a batch when the pointer arrays are given.
+template <typename C2>
+__device__ __forceinline__ void transpose_tile(const C2* __restrict__ src, C2* __restrict__ dst, uint32_t R,
+                                               uint32_t C) {
+  __shared__ C2 tile[32][33];
+  const uint32_t c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (uint32_t y = threadIdx.y; y < 32; y += blockDim.y) {
+    const uint32_t r = r0 + y, c = c0 + threadIdx.x;
+    if (r < R && c < C) tile[y][threadIdx.x] = src[(uint64_t)r * C + c];
+  }
+  __syncthreads();
+  for (uint32_t y = threadIdx.y; y < 32; y += blockDim.y) {
+    const uint32_t c = c0 + y, r = r0 + threadIdx.x;
+    if (r < R && c < C) dst[(uint64_t)c * R + r] = tile[threadIdx.x][y];
+  }
+}
+
 // Snapshot of the working block into block *d_k of the state
 // (std::copy_n of :130-132, taken after the power instead of before).
 template <typename C2>
-__global__ void k_snapshot(const C2* __restrict__ work, C2* __restrict__ state, uint64_t n, const int* d_k) {
-  const uint64_t k = (uint64_t)*d_k;
-  C2* __restrict__ dst = state + k * n;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-    dst[i] = work[i];
+__global__ void k_snapshot(const C2* __restrict__ work, C2* __restrict__ state, uint32_t Ca, uint32_t Cb,
+                           const int* d_k) {
+  transpose_tile(work, state + (uint64_t)*d_k * Ca * Cb, Cb, Ca);
+}
+
+// Block `block` of the state into the working block.
+template <typename C2>
+__global__ void k_load(C2* __restrict__ work, const C2* __restrict__ state, uint32_t Ca, uint32_t Cb, uint32_t block) {
+  transpose_tile(state + (uint64_t)block * Ca * Cb, work, Ca, Cb);
 }
 
 __global__ void k_advance(int* d_k) { *d_k += 1; }
 
 template <typename C2>
-__global__ void k_snapshot_batch(void* const* __restrict__ works, void* const* __restrict__ states, uint64_t n,
-                                 const int* d_k, uint32_t nmem) {
-  const uint64_t k = (uint64_t)*d_k;
-  const uint64_t total = n * nmem;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t m = i / n, e = i - m * n;
-    reinterpret_cast<C2*>(states[m])[k * n + e] = reinterpret_cast<const C2*>(works[m])[e];
-  }
+__global__ void k_snapshot_batch(void* const* __restrict__ works, void* const* __restrict__ states, uint32_t Ca,
+                                 uint32_t Cb, const int* d_k) {
+  const uint32_t m = blockIdx.z;
+  transpose_tile(reinterpret_cast<const C2*>(works[m]), reinterpret_cast<C2*>(states[m]) + (uint64_t)*d_k * Ca * Cb,
+                 Cb, Ca);
 }
 
 template <typename C2>
-__global__ void k_load_batch(void* const* __restrict__ works, void* const* __restrict__ states, uint64_t n,
-                             uint32_t block, uint32_t nmem) {
-  const uint64_t total = n * nmem;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t m = i / n, e = i - m * n;
-    reinterpret_cast<C2*>(works[m])[e] = reinterpret_cast<const C2*>(states[m])[(uint64_t)block * n + e];
-  }
+__global__ void k_load_batch(void* const* __restrict__ works, void* const* __restrict__ states, uint32_t Ca,
+                             uint32_t Cb, uint32_t block) {
+  const uint32_t m = blockIdx.z;
+  transpose_tile(reinterpret_cast<const C2*>(states[m]) + (uint64_t)block * Ca * Cb,
+                 reinterpret_cast<C2*>(works[m]), Ca, Cb);
 }
 
 // Continue the graph's while loop while the next power k + 1 is below `last`.
@@ -220,38 +243,47 @@ __global__ void k_continue_while(const int* d_k, int last, cudaGraphConditionalH
   cudaGraphSetConditional(h, *d_k + 1 < last ? 1u : 0u);
 }
 
-cudaError_t launch_snapshot(const void* work, void* state, uint64_t n, const int* d_k, int dtype, cudaStream_t s) {
-  uint64_t g = (n + 255) / 256;
-  if (g > 152 * 16) g = 152 * 16;
-  if (g < 1) g = 1;
+static dim3 transpose_grid(uint32_t R, uint32_t C, uint32_t members) {
+  return dim3((C + 31) / 32, (R + 31) / 32, members);
+}
+
+cudaError_t launch_snapshot(const void* work, void* state, uint32_t Ca, uint32_t Cb, const int* d_k, int dtype,
+                            cudaStream_t s) {
+  const dim3 g = transpose_grid(Cb, Ca, 1), b(32, 8);
   if (dtype == QPE_C128)
-    k_snapshot<double2><<<(uint32_t)g, 256, 0, s>>>((const double2*)work, (double2*)state, n, d_k);
+    k_snapshot<double2><<<g, b, 0, s>>>((const double2*)work, (double2*)state, Ca, Cb, d_k);
   else
-    k_snapshot<float2><<<(uint32_t)g, 256, 0, s>>>((const float2*)work, (float2*)state, n, d_k);
+    k_snapshot<float2><<<g, b, 0, s>>>((const float2*)work, (float2*)state, Ca, Cb, d_k);
   return cudaGetLastError();
 }
 
-static uint32_t grid_of(uint64_t n) {
-  uint64_t g = (n + 255) / 256;
-  if (g > 152 * 16) g = 152 * 16;
-  return (uint32_t)(g < 1 ? 1 : g);
-}
-
-cudaError_t launch_snapshot_batch(void* const* works, void* const* states, uint64_t n, const int* d_k, uint32_t nmem,
-                                  int dtype, cudaStream_t s) {
+cudaError_t launch_load(void* work, const void* state, uint32_t Ca, uint32_t Cb, uint32_t block, int dtype,
+                        cudaStream_t s) {
+  const dim3 g = transpose_grid(Ca, Cb, 1), b(32, 8);
   if (dtype == QPE_C128)
-    k_snapshot_batch<double2><<<grid_of(n * nmem), 256, 0, s>>>(works, states, n, d_k, nmem);
+    k_load<double2><<<g, b, 0, s>>>((double2*)work, (const double2*)state, Ca, Cb, block);
   else
-    k_snapshot_batch<float2><<<grid_of(n * nmem), 256, 0, s>>>(works, states, n, d_k, nmem);
+    k_load<float2><<<g, b, 0, s>>>((float2*)work, (const float2*)state, Ca, Cb, block);
   return cudaGetLastError();
 }
 
-cudaError_t launch_load_batch(void* const* works, void* const* states, uint64_t n, uint32_t block, uint32_t nmem,
-                              int dtype, cudaStream_t s) {
+cudaError_t launch_snapshot_batch(void* const* works, void* const* states, uint32_t Ca, uint32_t Cb, const int* d_k,
+                                  uint32_t nmem, int dtype, cudaStream_t s) {
+  const dim3 g = transpose_grid(Cb, Ca, nmem), b(32, 8);
   if (dtype == QPE_C128)
-    k_load_batch<double2><<<grid_of(n * nmem), 256, 0, s>>>(works, states, n, block, nmem);
+    k_snapshot_batch<double2><<<g, b, 0, s>>>(works, states, Ca, Cb, d_k);
   else
-    k_load_batch<float2><<<grid_of(n * nmem), 256, 0, s>>>(works, states, n, block, nmem);
+    k_snapshot_batch<float2><<<g, b, 0, s>>>(works, states, Ca, Cb, d_k);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_load_batch(void* const* works, void* const* states, uint32_t Ca, uint32_t Cb, uint32_t block,
+                              uint32_t nmem, int dtype, cudaStream_t s) {
+  const dim3 g = transpose_grid(Ca, Cb, nmem), b(32, 8);
+  if (dtype == QPE_C128)
+    k_load_batch<double2><<<g, b, 0, s>>>(works, states, Ca, Cb, block);
+  else
+    k_load_batch<float2><<<g, b, 0, s>>>(works, states, Ca, Cb, block);
   return cudaGetLastError();
 }
 

@@ -53,14 +53,19 @@ struct PassLaunch {
 constexpr uint32_t kCtaTileThreads = 128;
 size_t pass_stage_elems(const Pass& pass, uint32_t Ca, uint32_t Cb, uint32_t W);
 cudaError_t launch_pass(const PassLaunch& pl, int dtype, cudaStream_t s);
-cudaError_t launch_snapshot(const void* work, void* state, uint64_t block_elems, const int* d_k, int dtype,
+// The tile passes' working block is stored by columns (element (a, b) at
+// b * Ca + a); the register keeps row-major blocks. Snapshot: working block ->
+// block *d_k of the register; load: block `block` -> working block.
+cudaError_t launch_snapshot(const void* work, void* state, uint32_t Ca, uint32_t Cb, const int* d_k, int dtype,
                             cudaStream_t s);
+cudaError_t launch_load(void* work, const void* state, uint32_t Ca, uint32_t Cb, uint32_t block, int dtype,
+                        cudaStream_t s);
 cudaError_t launch_advance(int* d_k, cudaStream_t s);
-// Batches: working blocks -> block *d_k of each member's register; initial copy.
-cudaError_t launch_snapshot_batch(void* const* works, void* const* states, uint64_t n, const int* d_k, uint32_t nmem,
-                                  int dtype, cudaStream_t s);
-cudaError_t launch_load_batch(void* const* works, void* const* states, uint64_t n, uint32_t block, uint32_t nmem,
-                              int dtype, cudaStream_t s);
+// Batches: the same for every member of a class.
+cudaError_t launch_snapshot_batch(void* const* works, void* const* states, uint32_t Ca, uint32_t Cb, const int* d_k,
+                                  uint32_t nmem, int dtype, cudaStream_t s);
+cudaError_t launch_load_batch(void* const* works, void* const* states, uint32_t Ca, uint32_t Cb, uint32_t block,
+                              uint32_t nmem, int dtype, cudaStream_t s);
 // Sets the graph's while-loop condition to (*d_k + 1 < last).
 cudaError_t launch_continue_while(const int* d_k, int last, cudaGraphConditionalHandle h, cudaStream_t s);
 cudaError_t configure_pass_kernels(int dtype, size_t smem_bytes);
