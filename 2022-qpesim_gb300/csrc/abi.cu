@@ -233,8 +233,10 @@ static bool plan_resident_lean(const qpe_program* pr, const qpe_state* st, uint3
   const uint64_t stage = K > 1 ? 2 * Ca : 0;
   for (int with_meta = 1; with_meta >= 0; --with_meta)
     for (uint32_t wpc = 15; wpc >= 3; wpc -= 3) {
+      // block rows, group stages, the row-pointer table (Ca generic pointers), then the metadata
       const size_t head = (size_t)(Rk * Cb * esz + (wpc / 3) * stage * esz);
-      const size_t smem = with_meta ? ((head + 15) & ~(size_t)15) + meta : head;
+      const size_t rows = ((head + 15) & ~(size_t)15) + ((Ca * sizeof(void*) + 15) & ~(size_t)15);
+      const size_t smem = with_meta ? rows + meta : rows;
       if (smem + kResidentStaticSmem > st->ctx->smem_optin) continue;
       ri = ResidentInstance{};
       ri.Ca = (uint32_t)Ca;

@@ -489,10 +489,16 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
     else cl.sync();
   };
   auto gbar = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(gthreads) : "memory"); };
-  auto at = [&](uint32_t a, uint32_t b) -> C2* {
+  // Row a of the cluster-distributed block starts at rowp[a] (a generic pointer
+  // into the owning CTA's shared memory), so that a gather or scatter element
+  // costs one shared load instead of a division and an address mapping.
+  const size_t head = ((size_t)Rk * Cb + (size_t)ngrp * stage_elems) * sizeof(C2);
+  C2** rowp = reinterpret_cast<C2**>(smem_raw + ((head + 15) & ~(size_t)15));
+  for (uint32_t a = threadIdx.x; a < Ca; a += blockDim.x) {
     const uint32_t r = a / Rk;
-    return cta_ptr(blk, r, K) + (size_t)(a - r * Rk) * Cb + b;
-  };
+    rowp[a] = cta_ptr(blk, r, K) + (size_t)(a - r * Rk) * Cb;
+  }
+  auto at = [&](uint32_t a, uint32_t b) -> C2* { return rowp[a] + b; };
 
   const DevOp* ops = I.ops;
   const uint32_t* pool = I.pool;
@@ -500,8 +506,7 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
   const uint32_t* strA = I.strA;
   const uint32_t* strB = I.strB;
   if constexpr (MS) {
-    const size_t head = ((size_t)Rk * Cb + (size_t)ngrp * stage_elems) * sizeof(C2);
-    unsigned char* meta = smem_raw + ((head + 15) & ~(size_t)15);
+    unsigned char* meta = smem_raw + ((head + 15) & ~(size_t)15) + (((size_t)Ca * sizeof(C2*) + 15) & ~(size_t)15);
     DevOp* ops_s = reinterpret_cast<DevOp*>(meta);
     uint32_t* pool_s = reinterpret_cast<uint32_t*>(meta + (size_t)I.nops * sizeof(DevOp));
     Pass* passes_s = reinterpret_cast<Pass*>(pool_s + ((I.pool_words + 3u) & ~3u));
