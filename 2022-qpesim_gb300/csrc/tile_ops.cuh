@@ -384,25 +384,23 @@ __device__ __forceinline__ void chunked_line_ops(const DevOp* __restrict__ ops, 
     bool fast = true;
 #pragma unroll
     for (uint32_t k = 0; k < kPairChunk; ++k) {
-      da[k] = make_uint4(0u, 0u, 0u, 0u);
-      cc[k] = tt[k] = (R)0;
-      if (k < m) {
-        const uint32_t o = rev ? op1 - 1 - (i0 + k) : op0 + i0 + k;
-        const uint4* src = reinterpret_cast<const uint4*>(ops + o);
-        const uint4 a = __ldg(src), b = __ldg(src + 1);
-        const uint32_t kind = a.z & 0xffu;
-        const uint32_t count = kind == OPK_DIAG_ALL ? L : a.y;
-        fast = fast && a.w == OP_INLINE && count <= kPairTrips * jstep;
-        double c0 = __hiloint2double((int)b.y, (int)b.x), c1 = __hiloint2double((int)b.w, (int)b.z);
-        if (icoef) {
-          const double2 ic = __ldg(icoef + o);
-          c0 = ic.x;
-          c1 = ic.y;
-        }
-        da[k] = a;
-        cc[k] = (R)c0;
-        tt[k] = (R)c1;
+      // Every slot's descriptor is loaded (at a clamped index), so that the
+      // chunk's loads go out together instead of one after another behind guards.
+      const uint32_t o = rev ? op1 - 1 - (i0 + min(k, m - 1)) : op0 + i0 + min(k, m - 1);
+      const uint4* src = reinterpret_cast<const uint4*>(ops + o);
+      const uint4 a = __ldg(src), b = __ldg(src + 1);
+      const uint32_t kind = a.z & 0xffu;
+      const uint32_t count = kind == OPK_DIAG_ALL ? L : a.y;
+      if (k < m) fast = fast && a.w == OP_INLINE && count <= kPairTrips * jstep;
+      double c0 = __hiloint2double((int)b.y, (int)b.x), c1 = __hiloint2double((int)b.w, (int)b.z);
+      if (icoef) {
+        const double2 ic = __ldg(icoef + o);
+        c0 = ic.x;
+        c1 = ic.y;
       }
+      da[k] = a;
+      cc[k] = (R)c0;
+      tt[k] = (R)c1;
     }
     if (!fast) {
       run_line_ops<R, A, true>(ops, coef, pool, rev ? op1 - (i0 + m) : op0 + i0, rev ? op1 - i0 : op0 + i0 + m, rev,
@@ -418,27 +416,34 @@ __device__ __forceinline__ void chunked_line_ops(const DevOp* __restrict__ ops, 
       par[k] = okm[k] = 0;
 #pragma unroll
       for (uint32_t tr = 0; tr < kPairTrips; ++tr) p1[k][tr] = p2[k][tr] = nullptr;
-      if (k < m) {
-        const uint4 a = da[k];
+      {
+        const uint4 a = da[k];  // slots past the chunk hold its last term (loads only)
         const uint32_t kind = a.z & 0xffu, nc = (a.z >> 8) & 0xffu;
         uint32_t cm = 0;
         if (nc > 0) cm |= 1u << ((a.z >> 16) & 0xffu);
         if (nc > 1) cm |= 1u << (a.z >> 24);
-        const bool on = active && (lstr & cm) == cm;
+        const bool on = k < m && active && (lstr & cm) == cm;
         const uint32_t count = kind == OPK_DIAG_ALL ? L : a.y;
 #pragma unroll
         for (uint32_t tr = 0; tr < kPairTrips; ++tr) {
           const uint32_t j = jl + tr * jstep;
-          if (on && j < count) {
-            if (kind == OPK_PAIR) {
-              const uint2 x = __ldg(reinterpret_cast<const uint2*>(pool + a.x) + j);
+          // entries loaded at clamped indices as well; an empty table is not read
+          const uint32_t jj = count ? min(j, count - 1) : 0u;
+          const uint32_t* t = count ? pool + a.x : pool;
+          if (kind == OPK_PAIR) {
+            const uint2 x = __ldg(reinterpret_cast<const uint2*>(t) + jj);
+            if (on && j < count) {
               p1[k][tr] = &elem(x.x & 0x7fffffffu);
               p2[k][tr] = &elem(x.y);
               par[k] |= (x.x >> 31) << tr;
-            } else {
-              p1[k][tr] = &elem(kind == OPK_DIAG_LIST ? __ldg(pool + a.x + j) : j);
+              okm[k] |= 1u << tr;
             }
-            okm[k] |= 1u << tr;
+          } else {
+            const uint32_t e = kind == OPK_DIAG_LIST ? __ldg(t + jj) : jj;
+            if (on && j < count) {
+              p1[k][tr] = &elem(e);
+              okm[k] |= 1u << tr;
+            }
           }
         }
       }
