@@ -82,6 +82,34 @@ size_t resident_meta_bytes(uint32_t nops, uint32_t pool_words, uint32_t npasses,
          (size_t)(Ca + Cb) * 4;
 }
 
+// Stages the program's metadata in shared memory at `meta` (16-byte aligned), in
+// the order resident_meta_bytes counts it: term descriptors, index pool, passes,
+// alpha and beta line strings; the pointers are redirected to the copies. Every
+// thread of the CTA takes part; the caller's next barrier publishes the copies.
+__device__ __forceinline__ void stage_program(const ResidentInstance& I, unsigned char* meta, const DevOp*& ops,
+                                              const uint32_t*& pool, const Pass*& passes, const uint32_t*& strA,
+                                              const uint32_t*& strB) {
+  const uint32_t Ca = I.Ca, Cb = I.Cb;
+  DevOp* ops_s = reinterpret_cast<DevOp*>(meta);
+  uint32_t* pool_s = reinterpret_cast<uint32_t*>(meta + (size_t)I.nops * sizeof(DevOp));
+  Pass* passes_s = reinterpret_cast<Pass*>(pool_s + ((I.pool_words + 3u) & ~3u));
+  uint32_t* strA_s = reinterpret_cast<uint32_t*>(passes_s + I.npasses);
+  uint32_t* strB_s = strA_s + Ca;
+  const uint4* osrc = reinterpret_cast<const uint4*>(I.ops);
+  for (uint32_t i = threadIdx.x; i < I.nops * 2; i += blockDim.x) reinterpret_cast<uint4*>(ops_s)[i] = osrc[i];
+  for (uint32_t i = threadIdx.x; i < I.pool_words; i += blockDim.x) pool_s[i] = I.pool[i];
+  const uint32_t* psrc = reinterpret_cast<const uint32_t*>(I.passes);
+  for (uint32_t i = threadIdx.x; i < I.npasses * (uint32_t)(sizeof(Pass) / 4); i += blockDim.x)
+    reinterpret_cast<uint32_t*>(passes_s)[i] = psrc[i];
+  for (uint32_t i = threadIdx.x; i < Ca; i += blockDim.x) strA_s[i] = I.strA[i];
+  for (uint32_t i = threadIdx.x; i < Cb; i += blockDim.x) strB_s[i] = I.strB[i];
+  ops = ops_s;
+  pool = pool_s;
+  passes = passes_s;
+  strA = strA_s;
+  strB = strB_s;
+}
+
 constexpr uint32_t kGroupWarps = 4;
 
 // MS: the program's metadata (term descriptors, index pool, passes, line strings)
@@ -128,25 +156,7 @@ __global__ void __launch_bounds__(512) k_resident(const ResidentInstance* __rest
   const uint32_t* strB = I.strB;
   if constexpr (MS) {
     const size_t head = ((size_t)Rk * Cb + (size_t)wpc * stage_elems) * sizeof(C2);
-    unsigned char* meta = smem_raw + ((head + 15) & ~(size_t)15);
-    DevOp* ops_s = reinterpret_cast<DevOp*>(meta);
-    uint32_t* pool_s = reinterpret_cast<uint32_t*>(meta + (size_t)I.nops * sizeof(DevOp));
-    Pass* passes_s = reinterpret_cast<Pass*>(pool_s + ((I.pool_words + 3u) & ~3u));
-    uint32_t* strA_s = reinterpret_cast<uint32_t*>(passes_s + I.npasses);
-    uint32_t* strB_s = strA_s + Ca;
-    const uint4* osrc = reinterpret_cast<const uint4*>(I.ops);
-    for (uint32_t i = threadIdx.x; i < I.nops * 2; i += blockDim.x) reinterpret_cast<uint4*>(ops_s)[i] = osrc[i];
-    for (uint32_t i = threadIdx.x; i < I.pool_words; i += blockDim.x) pool_s[i] = I.pool[i];
-    const uint32_t* psrc = reinterpret_cast<const uint32_t*>(I.passes);
-    for (uint32_t i = threadIdx.x; i < I.npasses * (uint32_t)(sizeof(Pass) / 4); i += blockDim.x)
-      reinterpret_cast<uint32_t*>(passes_s)[i] = psrc[i];
-    for (uint32_t i = threadIdx.x; i < Ca; i += blockDim.x) strA_s[i] = I.strA[i];
-    for (uint32_t i = threadIdx.x; i < Cb; i += blockDim.x) strB_s[i] = I.strB[i];
-    ops = ops_s;
-    pool = pool_s;
-    passes = passes_s;
-    strA = strA_s;
-    strB = strB_s;
+    stage_program(I, smem_raw + ((head + 15) & ~(size_t)15), ops, pool, passes, strA, strB);
   }
   constexpr bool G = !MS;
   // distributed-shared-memory loads in flight per lane in the tile gathers
@@ -337,25 +347,7 @@ __global__ void __launch_bounds__(512) k_resident_group(const ResidentInstance* 
   const uint32_t* strB = I.strB;
   if constexpr (MS) {
     const size_t head = ((size_t)Rk * Cb + (size_t)ngrp * stage_elems) * sizeof(C2);
-    unsigned char* meta = smem_raw + ((head + 15) & ~(size_t)15);
-    DevOp* ops_s = reinterpret_cast<DevOp*>(meta);
-    uint32_t* pool_s = reinterpret_cast<uint32_t*>(meta + (size_t)I.nops * sizeof(DevOp));
-    Pass* passes_s = reinterpret_cast<Pass*>(pool_s + ((I.pool_words + 3u) & ~3u));
-    uint32_t* strA_s = reinterpret_cast<uint32_t*>(passes_s + I.npasses);
-    uint32_t* strB_s = strA_s + Ca;
-    const uint4* osrc = reinterpret_cast<const uint4*>(I.ops);
-    for (uint32_t i = threadIdx.x; i < I.nops * 2; i += blockDim.x) reinterpret_cast<uint4*>(ops_s)[i] = osrc[i];
-    for (uint32_t i = threadIdx.x; i < I.pool_words; i += blockDim.x) pool_s[i] = I.pool[i];
-    const uint32_t* psrc = reinterpret_cast<const uint32_t*>(I.passes);
-    for (uint32_t i = threadIdx.x; i < I.npasses * (uint32_t)(sizeof(Pass) / 4); i += blockDim.x)
-      reinterpret_cast<uint32_t*>(passes_s)[i] = psrc[i];
-    for (uint32_t i = threadIdx.x; i < Ca; i += blockDim.x) strA_s[i] = I.strA[i];
-    for (uint32_t i = threadIdx.x; i < Cb; i += blockDim.x) strB_s[i] = I.strB[i];
-    ops = ops_s;
-    pool = pool_s;
-    passes = passes_s;
-    strA = strA_s;
-    strB = strB_s;
+    stage_program(I, smem_raw + ((head + 15) & ~(size_t)15), ops, pool, passes, strA, strB);
   }
   constexpr bool G = !MS;
   constexpr int kDepth = sizeof(R) == 8 ? 2 : 4;
@@ -505,27 +497,9 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
   const Pass* passes = I.passes;
   const uint32_t* strA = I.strA;
   const uint32_t* strB = I.strB;
-  if constexpr (MS) {
-    unsigned char* meta = smem_raw + ((head + 15) & ~(size_t)15) + (((size_t)Ca * sizeof(C2*) + 15) & ~(size_t)15);
-    DevOp* ops_s = reinterpret_cast<DevOp*>(meta);
-    uint32_t* pool_s = reinterpret_cast<uint32_t*>(meta + (size_t)I.nops * sizeof(DevOp));
-    Pass* passes_s = reinterpret_cast<Pass*>(pool_s + ((I.pool_words + 3u) & ~3u));
-    uint32_t* strA_s = reinterpret_cast<uint32_t*>(passes_s + I.npasses);
-    uint32_t* strB_s = strA_s + Ca;
-    const uint4* osrc = reinterpret_cast<const uint4*>(I.ops);
-    for (uint32_t i = threadIdx.x; i < I.nops * 2; i += blockDim.x) reinterpret_cast<uint4*>(ops_s)[i] = osrc[i];
-    for (uint32_t i = threadIdx.x; i < I.pool_words; i += blockDim.x) pool_s[i] = I.pool[i];
-    const uint32_t* psrc = reinterpret_cast<const uint32_t*>(I.passes);
-    for (uint32_t i = threadIdx.x; i < I.npasses * (uint32_t)(sizeof(Pass) / 4); i += blockDim.x)
-      reinterpret_cast<uint32_t*>(passes_s)[i] = psrc[i];
-    for (uint32_t i = threadIdx.x; i < Ca; i += blockDim.x) strA_s[i] = I.strA[i];
-    for (uint32_t i = threadIdx.x; i < Cb; i += blockDim.x) strB_s[i] = I.strB[i];
-    ops = ops_s;
-    pool = pool_s;
-    passes = passes_s;
-    strA = strA_s;
-    strB = strB_s;
-  }
+  if constexpr (MS)
+    stage_program(I, smem_raw + ((head + 15) & ~(size_t)15) + (((size_t)Ca * sizeof(C2*) + 15) & ~(size_t)15), ops,
+                  pool, passes, strA, strB);
   constexpr bool G = !MS;
   constexpr int kDepth = sizeof(R) == 8 ? 2 : 4;
   const bool in_group = grp < ngrp;  // threads past the last whole group only join the CTA barriers
