@@ -37,22 +37,22 @@ import __graft_entry__ as graft  # noqa: E402
 FP64_PEAK_TFLOPS = 1.19  # measured FP64 FMA throughput of this GB300 (own probe; not in MEASURED_PEAKS.json)
 
 WORKLOADS = {
-    # BASELINE configs[1]: plain QPE in FP64.
+    # Plain QPE in FP64: n = 16, N = 8, 10 ancilla qubits (the default workload).
     "plain-n16": dict(n=16, N=8, P=10, dt=0.05, order=2, steps=4, dtype="c128", seed=0,
                       desc="Plain QPE, FP64: n=16 spin-orbitals, N=8, 10 ancilla qubits, complex128, 2nd-order "
                            "Trotter dt=0.05, 4 steps per power, Hartree-Fock start"),
-    # The reference's own CPU-runnable case (BASELINE configs[0]), a parity case.
+    # The reference's own CPU-runnable case: n = 8, N = 4, 6 ancilla qubits (a parity case).
     "plain-n8": dict(n=8, N=4, P=6, dt=0.1, order=1, steps=1, dtype="c128", seed=0,
                      desc="Plain QPE, FP64: n=8, N=4, 6 ancilla qubits, 1st-order Trotter dt=0.1"),
 }
-# BASELINE configs[3]: the batching form.
+# The batching form: 256 Hamiltonians of n = 12..20.
 WORKLOADS["batched-256"] = dict(batch=True, count=256, sizes=(12, 14, 16, 18, 20), P=6, dt=0.05, order=1, steps=1,
                                 dtype="c64", seed=2024, check_c128=True,
                                 desc="Batching form: 256 seeded Hamiltonians, n uniform in {12,14,16,18,20}, N=n/2 "
                                      "(odd N split ceil/floor over the spins), 6 ancilla qubits, complex64 with FP64 "
                                      "coefficients and histograms, 1st-order Trotter dt=0.05, Hartree-Fock starts, "
                                      "one graph launch per step")
-# BASELINE configs[2]: the precision form, one large instance in complex64.
+# The precision form: one n = 24, N = 12 instance in complex64.
 WORKLOADS["precision-n24"] = dict(n=24, N=12, P=8, dt=0.05, order=1, steps=1, dtype="c64", seed=0, check_c128=True,
                                   desc="Precision form: n=24, N=12 (853,776 amplitudes per block in the reference's "
                                        "Na=Nb layout), 8 ancilla qubits, complex64 state with FP64 coefficients, "
@@ -63,7 +63,7 @@ WORKLOADS["precision-n24"] = dict(n=24, N=12, P=8, dt=0.05, order=1, steps=1, dt
 WORKLOADS["batched-32"] = dict(WORKLOADS["batched-256"], count=32,
                                desc="Batching form, 32-instance draw (profiling case): n uniform in "
                                     "{12,14,16,18,20}, N=n/2, 6 ancilla qubits, complex64, dt=0.05")
-# BASELINE configs[4]: the learned initial-state form.
+# The learned initial-state form: n = 20, N = 10.
 WORKLOADS["learned-n20"] = dict(learned=True, n=20, N=10, P=10, P_data=6, dt=0.05, train=512, held_out=64,
                                 train_steps=3000, batch=65536, lr=1e-3, seed=31337, dtype="c64",
                                 desc="Learned initial state: n=20, N=10 (63,504 amplitudes per block in the "
