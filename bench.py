@@ -80,13 +80,13 @@ DEFAULT_WORKLOAD = "plain-n16"
 # DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum) from the ncu captures summarised under profiles/.
 MEASURED_TRAFFIC = {
-    "plain-n16": (495_872 + 1_024, "k_resident, cluster of 16: one launch runs every power; the capture of a "
-                                   "2-power launch read the block and the program once (0.50 MB) and wrote 1 KB, "
-                                   "the snapshots staying in L2 (profiles/k_resident_cluster16_plain_n16.md)"),
-    "precision-n24": (6_863_275, "k_pass MIX launch, one tile per CTA: the 6.8 MB working block read once, cold "
-                                 "cache under ncu (profiles/k_pass_precision_n24.md)"),
-    "batched-256": (28_600_000, "k_pass MIX launch: 3.57 MB for the 32-instance draw, scaled by the 8x members "
-                                "per launch (profiles/k_pass_batched32.md)"),
+    "plain-n16": (338_944, "k_resident_lean, cluster of 16: one launch runs every power; the capture of a "
+                           "2-power launch read the block and the program once (0.34 MB) and wrote nothing back to "
+                           "DRAM, the snapshots staying in L2 (ncu capture of the same kernel, small case)"),
+    "precision-n24": (6_876_160, "k_pass MIX launch, one tile per CTA: the 6.9 MB working block read once, cold "
+                                 "cache under ncu (capture at P = 3; the working block is the same at any P)"),
+    "batched-256": (28_700_000, "k_pass MIX launch: 3.59 MB for the 32-instance draw, scaled by the 8x members "
+                                "per launch"),
 }
 
 
