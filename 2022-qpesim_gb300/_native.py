@@ -113,6 +113,14 @@ PROTOTYPES = {
     "qpe_mlp_gradients": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                     C.POINTER(C.c_float), C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "qpe_mlp_tensor_flops_per_step": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "qpe_mlp_create2": (C.c_int, [_vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.POINTER(_vp)]),
+    "qpe_mlp_set_data2": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                    C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint64]),
+    "qpe_mlp_forward2": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.c_uint64,
+                                   C.POINTER(C.c_float)]),
+    "qpe_mlp_gradients2": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                     C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32, C.POINTER(C.c_float),
+                                     C.POINTER(C.c_float)]),
     "qpe_gemm_bf16": (C.c_int, [_vp, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint16),
                                 C.POINTER(C.c_uint16), C.POINTER(C.c_float), C.c_uint32]),
     "qpe_ham_create": (C.c_int, [C.POINTER(_vp)]),

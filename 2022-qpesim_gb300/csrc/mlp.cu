@@ -241,21 +241,27 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
 }
 
 // Row b of the batch: sample idx (random when `sample`, else b) -> input
-// features (bit j of the occupation string as 0 / 1, zero past n_bits) and the
-// sample's targets. Rows past `count` are zero with weight 0.
-__global__ void k_gather_batch(const uint64_t* __restrict__ bits, const float* __restrict__ tla,
-                               const float* __restrict__ tph, const float* __restrict__ tw, uint64_t nsamples,
-                               uint32_t count, uint32_t Bp, uint32_t n_bits, int sample, uint64_t seed,
-                               const uint64_t* __restrict__ step, bf16* __restrict__ X0, float* __restrict__ bla,
-                               float* __restrict__ bph, float* __restrict__ bw) {
+// features (bit j of the occupation string as 0 / 1 for j < n_bits, then the
+// sample's n_feat extra features, zero past them) and the sample's targets. Rows
+// past `count` are zero with weight 0.
+__global__ void k_gather_batch(const uint64_t* __restrict__ bits, const float* __restrict__ feats, uint32_t n_feat,
+                               const float* __restrict__ tla, const float* __restrict__ tph,
+                               const float* __restrict__ tw, uint64_t nsamples, uint32_t count, uint32_t Bp,
+                               uint32_t n_bits, int sample, uint64_t seed, const uint64_t* __restrict__ step,
+                               bf16* __restrict__ X0, float* __restrict__ bla, float* __restrict__ bph,
+                               float* __restrict__ bw) {
   const uint32_t b = blockIdx.x;
   if (b >= Bp) return;
   uint64_t idx = b;
   const bool live = b < count;
   if (live && sample) idx = mix64(seed ^ mix64(*step * 0x9e3779b97f4a7c15ull + b)) % nsamples;
   const uint64_t x = live ? bits[idx] : 0ull;
-  for (uint32_t j = threadIdx.x; j < 64; j += blockDim.x)
-    X0[(size_t)b * 64 + j] = __float2bfloat16_rn((live && j < n_bits && ((x >> j) & 1ull)) ? 1.f : 0.f);
+  for (uint32_t j = threadIdx.x; j < 64; j += blockDim.x) {
+    float v = 0.f;
+    if (live && j < n_bits) v = ((x >> j) & 1ull) ? 1.f : 0.f;
+    else if (live && j < n_bits + n_feat) v = feats[idx * n_feat + (j - n_bits)];
+    X0[(size_t)b * 64 + j] = __float2bfloat16_rn(v);
+  }
   if (threadIdx.x == 0) {
     bla[b] = live && tla ? tla[idx] : 0.f;
     bph[b] = live && tph ? tph[idx] : 0.f;
@@ -462,7 +468,7 @@ using namespace qpe;
 
 struct qpe_mlp {
   qpe_context* ctx = nullptr;
-  uint32_t n_bits = 0, Bp = 0;
+  uint32_t n_bits = 0, n_feat = 0, Bp = 0;  // inputs: n_bits occupations, then n_feat features
   static constexpr uint32_t K0 = 64, H = 256, NO = 16;
   // FP32 master parameters, Adam moments and gradients, one flat array each.
   DevBuf params, mom1, mom2, grads;
@@ -473,7 +479,7 @@ struct qpe_mlp {
   DevBuf X0T, H1T, H2T, H3T, dYT, dZ1T, dZ2T, dZ3T;
   DevBuf bla, bph, bw, loss, err, step, colpart, splitk;
   // training set
-  DevBuf dbits, dla, dph, dw;
+  DevBuf dbits, dfeat, dla, dph, dw;
   uint64_t nsamples = 0;
   std::vector<Gemm> fwd, bwd, wgrad;
   cudaGraphExec_t train_exec = nullptr;
@@ -654,15 +660,22 @@ static void use_ctx(qpe_context* ctx) {
 extern "C" {
 
 int qpe_mlp_create(qpe_context* ctx, uint32_t n_bits, uint32_t batch, uint64_t seed, qpe_mlp** out) {
+  return qpe_mlp_create2(ctx, n_bits, 0, batch, seed, out);
+}
+
+int qpe_mlp_create2(qpe_context* ctx, uint32_t n_bits, uint32_t n_feat, uint32_t batch, uint64_t seed,
+                    qpe_mlp** out) {
   return guard([&] {
     use_ctx(ctx);
     if (!out) throw Error(QPE_ERR_INVALID, "null output");
     if (n_bits == 0 || n_bits > 64) throw Error(QPE_ERR_INVALID, "n_bits must be in 1..64");
+    if (n_feat > 64 - n_bits) throw Error(QPE_ERR_INVALID, "n_bits + n_feat must be at most 64");
     if (batch == 0 || batch % 128 || batch > (1u << 20)) throw Error(QPE_ERR_INVALID, "batch must be a multiple of 128");
     auto m = new qpe_mlp();
     try {
       m->ctx = ctx;
       m->n_bits = n_bits;
+      m->n_feat = n_feat;
       m->Bp = batch;
       mlp_alloc(m);
       // Uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights from a seeded generator,
@@ -677,8 +690,9 @@ int qpe_mlp_create(qpe_context* ctx, uint32_t n_bits, uint32_t batch, uint64_t s
         z ^= z >> 31;
         return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
       };
+      const uint32_t n_in = n_bits + n_feat;
       for (uint32_t o = 0; o < 256; ++o)
-        for (uint32_t i = 0; i < n_bits; ++i) p[qpe_mlp::oW1 + o * 64 + i] = (float)(uni() / std::sqrt((double)n_bits));
+        for (uint32_t i = 0; i < n_in; ++i) p[qpe_mlp::oW1 + o * 64 + i] = (float)(uni() / std::sqrt((double)n_in));
       for (size_t i = 0; i < 256 * 256; ++i) p[qpe_mlp::oW2 + i] = (float)(uni() / 16.0);
       for (size_t i = 0; i < 256 * 256; ++i) p[qpe_mlp::oW3 + i] = (float)(uni() / 16.0);
       for (size_t i = 0; i < 2 * 256; ++i) p[qpe_mlp::oW4 + i] = (float)(uni() / 16.0);
@@ -724,9 +738,9 @@ int qpe_mlp_set_params(qpe_mlp* m, const float* host) {
     if (!m || !host) throw Error(QPE_ERR_INVALID, "null argument");
     use_ctx(m->ctx);
     std::vector<float> p(host, host + qpe_mlp::nparams);
-    // keep the padding zero: input columns past n_bits, output rows past 1
+    // keep the padding zero: input columns past n_bits + n_feat, output rows past 1
     for (uint32_t o = 0; o < 256; ++o)
-      for (uint32_t i = m->n_bits; i < 64; ++i) p[qpe_mlp::oW1 + o * 64 + i] = 0.f;
+      for (uint32_t i = m->n_bits + m->n_feat; i < 64; ++i) p[qpe_mlp::oW1 + o * 64 + i] = 0.f;
     for (size_t i = 2 * 256; i < 16 * 256; ++i) p[qpe_mlp::oW4 + i] = 0.f;
     for (size_t i = 2; i < 16; ++i) p[qpe_mlp::ob4 + i] = 0.f;
     QPE_CK(cudaMemcpy(m->params.p, p.data(), p.size() * 4, cudaMemcpyHostToDevice));
@@ -737,9 +751,22 @@ int qpe_mlp_set_params(qpe_mlp* m, const float* host) {
 
 int qpe_mlp_set_data(qpe_mlp* m, const uint64_t* bits, const float* log_abs, const float* phase, const float* weight,
                      uint64_t count) {
+  return qpe_mlp_set_data2(m, bits, nullptr, log_abs, phase, weight, count);
+}
+
+// The model's feature count must be 0 or the caller must give the features.
+static void check_feats(const qpe_mlp* m, const float* feats) {
+  if (m->n_feat && !feats) throw Error(QPE_ERR_INVALID, "the model takes features: pass them");
+}
+
+int qpe_mlp_set_data2(qpe_mlp* m, const uint64_t* bits, const float* feats, const float* log_abs, const float* phase,
+                      const float* weight, uint64_t count) {
   return guard([&] {
     if (!m || !bits || !log_abs || !phase || !weight || !count) throw Error(QPE_ERR_INVALID, "null argument");
+    check_feats(m, feats);
     use_ctx(m->ctx);
+    m->dfeat.alloc(std::max<uint64_t>(1, count * m->n_feat) * 4);
+    if (m->n_feat) QPE_CK(cudaMemcpy(m->dfeat.p, feats, count * m->n_feat * 4, cudaMemcpyHostToDevice));
     m->dbits.alloc(count * 8);
     m->dla.alloc(count * 4);
     m->dph.alloc(count * 4);
@@ -767,8 +794,9 @@ int qpe_mlp_train(qpe_mlp* m, uint32_t steps, float lr, uint64_t seed, float* lo
       ++m->adam_t;
       const float c1 = 1.0f / (1.0f - std::pow(0.9f, (float)m->adam_t));
       const float c2 = 1.0f / (1.0f - std::pow(0.999f, (float)m->adam_t));
-      k_gather_batch<<<m->Bp, 64, 0, s>>>(m->dbits.as<uint64_t>(), m->dla.as<float>(), m->dph.as<float>(),
-                                           m->dw.as<float>(), m->nsamples, m->Bp, m->Bp, m->n_bits, 1, seed,
+      k_gather_batch<<<m->Bp, 64, 0, s>>>(m->dbits.as<uint64_t>(), m->dfeat.as<float>(), m->n_feat,
+                                           m->dla.as<float>(), m->dph.as<float>(), m->dw.as<float>(), m->nsamples,
+                                           m->Bp, m->Bp, m->n_bits, 1, seed,
                                            m->step.as<uint64_t>(), m->X0.as<bf16>(), m->bla.as<float>(),
                                            m->bph.as<float>(), m->bw.as<float>());
       QPE_CK(cudaGetLastError());
@@ -784,18 +812,26 @@ int qpe_mlp_train(qpe_mlp* m, uint32_t steps, float lr, uint64_t seed, float* lo
 }
 
 int qpe_mlp_forward(qpe_mlp* m, const uint64_t* bits, uint64_t count, float* out) {
+  return qpe_mlp_forward2(m, bits, nullptr, count, out);
+}
+
+int qpe_mlp_forward2(qpe_mlp* m, const uint64_t* bits, const float* feats, uint64_t count, float* out) {
   return guard([&] {
     if (!m || (count && (!bits || !out))) throw Error(QPE_ERR_INVALID, "null argument");
+    if (count) check_feats(m, feats);
     use_ctx(m->ctx);
     cudaStream_t s = m->ctx->stream;
-    DevBuf db;
+    DevBuf db, df;
     db.alloc(std::max<uint64_t>(count, 1) * 8);
     QPE_CK(cudaMemcpy(db.p, bits, count * 8, cudaMemcpyHostToDevice));
+    df.alloc(std::max<uint64_t>(1, count * m->n_feat) * 4);
+    if (m->n_feat && count) QPE_CK(cudaMemcpy(df.p, feats, count * m->n_feat * 4, cudaMemcpyHostToDevice));
     std::vector<float> y((size_t)m->Bp * 16);
     for (uint64_t c0 = 0; c0 < count; c0 += m->Bp) {
       const uint32_t n = (uint32_t)std::min<uint64_t>(m->Bp, count - c0);
-      k_gather_batch<<<m->Bp, 64, 0, s>>>(db.as<uint64_t>() + c0, nullptr, nullptr, nullptr, n, n, m->Bp, m->n_bits,
-                                           0, 0, m->step.as<uint64_t>(), m->X0.as<bf16>(), m->bla.as<float>(),
+      k_gather_batch<<<m->Bp, 64, 0, s>>>(db.as<uint64_t>() + c0, df.as<float>() + c0 * m->n_feat, m->n_feat,
+                                           nullptr, nullptr, nullptr, n, n, m->Bp, m->n_bits, 0, 0,
+                                           m->step.as<uint64_t>(), m->X0.as<bf16>(), m->bla.as<float>(),
                                            m->bph.as<float>(), m->bw.as<float>());
       QPE_CK(cudaGetLastError());
       forward(m, s);
@@ -812,12 +848,20 @@ int qpe_mlp_forward(qpe_mlp* m, const uint64_t* bits, uint64_t count, float* out
 
 int qpe_mlp_gradients(qpe_mlp* m, const uint64_t* bits, const float* log_abs, const float* phase,
                       const float* weight, uint32_t count, float* grads, float* loss) {
+  return qpe_mlp_gradients2(m, bits, nullptr, log_abs, phase, weight, count, grads, loss);
+}
+
+int qpe_mlp_gradients2(qpe_mlp* m, const uint64_t* bits, const float* feats, const float* log_abs, const float* phase,
+                       const float* weight, uint32_t count, float* grads, float* loss) {
   return guard([&] {
     if (!m || !bits || !log_abs || !phase || !weight || !grads) throw Error(QPE_ERR_INVALID, "null argument");
     if (count == 0 || count > m->Bp) throw Error(QPE_ERR_INVALID, "count must be in 1..batch");
+    check_feats(m, feats);
     use_ctx(m->ctx);
     cudaStream_t s = m->ctx->stream;
-    DevBuf db, dl, dp, dw;
+    DevBuf db, dl, dp, dw, df;
+    df.alloc(std::max<uint64_t>(1, (uint64_t)count * m->n_feat) * 4);
+    if (m->n_feat) QPE_CK(cudaMemcpy(df.p, feats, (size_t)count * m->n_feat * 4, cudaMemcpyHostToDevice));
     db.alloc(count * 8);
     dl.alloc(count * 4);
     dp.alloc(count * 4);
@@ -827,9 +871,10 @@ int qpe_mlp_gradients(qpe_mlp* m, const uint64_t* bits, const float* log_abs, co
     QPE_CK(cudaMemcpy(dp.p, phase, count * 4, cudaMemcpyHostToDevice));
     QPE_CK(cudaMemcpy(dw.p, weight, count * 4, cudaMemcpyHostToDevice));
     QPE_CK(cudaMemsetAsync(m->loss.p, 0, 4, s));
-    k_gather_batch<<<m->Bp, 64, 0, s>>>(db.as<uint64_t>(), dl.as<float>(), dp.as<float>(), dw.as<float>(), count,
-                                         count, m->Bp, m->n_bits, 0, 0, m->step.as<uint64_t>(), m->X0.as<bf16>(),
-                                         m->bla.as<float>(), m->bph.as<float>(), m->bw.as<float>());
+    k_gather_batch<<<m->Bp, 64, 0, s>>>(db.as<uint64_t>(), df.as<float>(), m->n_feat, dl.as<float>(), dp.as<float>(),
+                                         dw.as<float>(), count, count, m->Bp, m->n_bits, 0, 0,
+                                         m->step.as<uint64_t>(), m->X0.as<bf16>(), m->bla.as<float>(),
+                                         m->bph.as<float>(), m->bw.as<float>());
     QPE_CK(cudaGetLastError());
     forward(m, s);
     backward(m, count, s, m->loss.as<float>());

@@ -64,14 +64,15 @@ def _fp(a):
 
 
 class AmplitudeMLP:
-    """Occupation string -> (log|a|, phase); n_bits inputs, 3 x 256 GELU, BF16."""
+    """Occupation string (and n_feat extra features) -> (log|a|, phase); n_bits +
+    n_feat inputs, 3 x 256 GELU, BF16."""
 
-    def __init__(self, n_bits: int, batch: int = 8192, seed: int = 0, device: int = 0):
+    def __init__(self, n_bits: int, batch: int = 8192, seed: int = 0, device: int = 0, n_feat: int = 0):
         self._lib = N.lib()
         h = C.c_void_p()
-        N.check(self._lib.qpe_mlp_create(N.context(device), n_bits, batch, seed, C.byref(h)))
+        N.check(self._lib.qpe_mlp_create2(N.context(device), n_bits, n_feat, batch, seed, C.byref(h)))
         self._h = h
-        self.n_bits, self.batch = n_bits, batch
+        self.n_bits, self.n_feat, self.batch = n_bits, n_feat, batch
         n = C.c_uint64()
         N.check(self._lib.qpe_mlp_num_params(h, C.byref(n)))
         self.num_params = n.value
@@ -92,30 +93,41 @@ class AmplitudeMLP:
         assert p.size == self.num_params
         N.check(self._lib.qpe_mlp_set_params(self._h, _fp(p)))
 
-    def set_data(self, bits, log_abs, phase, weight) -> None:
+    def _feats(self, feats, count):
+        if self.n_feat == 0:
+            return None
+        f = np.ascontiguousarray(feats, np.float32).reshape(count, self.n_feat)
+        return f
+
+    def set_data(self, bits, log_abs, phase, weight, feats=None) -> None:
         bits = np.ascontiguousarray(bits, np.uint64)
         la, ph, w = (np.ascontiguousarray(x, np.float32) for x in (log_abs, phase, weight))
-        N.check(self._lib.qpe_mlp_set_data(self._h, bits.ctypes.data_as(C.POINTER(C.c_uint64)), _fp(la), _fp(ph),
-                                           _fp(w), bits.size))
+        f = self._feats(feats, bits.size)
+        N.check(self._lib.qpe_mlp_set_data2(self._h, bits.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                            _fp(f) if f is not None else None, _fp(la), _fp(ph), _fp(w), bits.size))
 
     def train(self, steps: int, lr: float = 1e-3, seed: int = 0) -> np.ndarray:
         losses = np.zeros(steps, np.float32)
         N.check(self._lib.qpe_mlp_train(self._h, steps, lr, seed, _fp(losses)))
         return losses
 
-    def forward(self, bits) -> np.ndarray:
+    def forward(self, bits, feats=None) -> np.ndarray:
         bits = np.ascontiguousarray(bits, np.uint64)
         out = np.zeros((bits.size, 2), np.float32)
-        N.check(self._lib.qpe_mlp_forward(self._h, bits.ctypes.data_as(C.POINTER(C.c_uint64)), bits.size, _fp(out)))
+        f = self._feats(feats, bits.size)
+        N.check(self._lib.qpe_mlp_forward2(self._h, bits.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                           _fp(f) if f is not None else None, bits.size, _fp(out)))
         return out
 
-    def gradients(self, bits, log_abs, phase, weight):
+    def gradients(self, bits, log_abs, phase, weight, feats=None):
         bits = np.ascontiguousarray(bits, np.uint64)
         la, ph, w = (np.ascontiguousarray(x, np.float32) for x in (log_abs, phase, weight))
         g = np.zeros(self.num_params, np.float32)
         loss = np.zeros(1, np.float32)
-        N.check(self._lib.qpe_mlp_gradients(self._h, bits.ctypes.data_as(C.POINTER(C.c_uint64)), _fp(la), _fp(ph),
-                                            _fp(w), bits.size, _fp(g), _fp(loss)))
+        f = self._feats(feats, bits.size)
+        N.check(self._lib.qpe_mlp_gradients2(self._h, bits.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                             _fp(f) if f is not None else None, _fp(la), _fp(ph), _fp(w), bits.size,
+                                             _fp(g), _fp(loss)))
         return g, float(loss[0])
 
     def tensor_flops_per_step(self) -> float:
@@ -167,9 +179,39 @@ def state_targets(psi: np.ndarray, floor: float = 1e-6):
             (a * a * len(psi) + 0.05).astype(np.float32))
 
 
-def proposed_state(model: AmplitudeMLP, strings: np.ndarray) -> np.ndarray:
-    """The model's state over `strings`, normalised to 1."""
-    out = model.forward(strings).astype(np.float64)
+# Extra inputs of the learned model per occupation string: its diagonal energy
+# <x|H|x> under the string's Hamiltonian, as z = (E - E_min) / std over the
+# sector (clipped at 8) and exp(-z).
+N_DIAG_FEATURES = 2
+
+
+def diagonal_energies(hamiltonian, strings: np.ndarray) -> np.ndarray:
+    """<x|H|x> of every string x: the pp terms h_p n_p and the pqqp terms
+    h_pq n_p n_q (the terms that act diagonally; bit p of x is spin orbital p)."""
+    raw = hamiltonian.PrintIndexedSegmentedHamiltonianTerms()
+    nso = 2 * hamiltonian.num_orbitals()
+    h1 = np.zeros(nso)
+    for (p, _), v in raw[0]:
+        h1[p] += v
+    J = np.zeros((nso, nso))
+    for (p, q, _, _), v in raw[2]:
+        J[p, q] += v
+    occ = ((np.asarray(strings, np.uint64)[:, None] >> np.arange(nso, dtype=np.uint64)[None, :])
+           & np.uint64(1)).astype(np.float64)
+    return occ @ h1 + np.einsum("ij,ij->i", occ @ J, occ)
+
+
+def diagonal_features(hamiltonian, strings: np.ndarray) -> np.ndarray:
+    """The model's extra inputs for `strings` under `hamiltonian` ([len, 2] float32)."""
+    e = diagonal_energies(hamiltonian, strings)
+    z = (e - e.min()) / max(float(e.std()), 1e-12)
+    return np.stack([np.minimum(z, 8.0), np.exp(-z)], axis=1).astype(np.float32)
+
+
+def proposed_state(model: AmplitudeMLP, strings: np.ndarray, feats=None) -> np.ndarray:
+    """The model's state over `strings` (with the features of their Hamiltonian
+    when the model takes features), normalised to 1."""
+    out = model.forward(strings, feats).astype(np.float64)
     amp = np.exp(out[:, 0] - out[:, 0].max()) * np.exp(1j * out[:, 1])
     return amp / np.linalg.norm(amp)
 

@@ -67,7 +67,8 @@ WORKLOADS["batched-32"] = dict(WORKLOADS["batched-256"], count=32,
 WORKLOADS["learned-n20"] = dict(learned=True, n=20, N=10, P=10, P_data=6, dt=0.05, train=512, held_out=64,
                                 train_steps=3000, batch=65536, lr=1e-3, seed=31337, dtype="c64",
                                 desc="Learned initial state: n=20, N=10 (63,504 amplitudes per block in the "
-                                     "reference's Na=Nb layout), 10 ancilla qubits for evaluation; MLP 20 -> 3 x 256 "
+                                     "reference's Na=Nb layout), 10 ancilla qubits for evaluation; MLP (20 occupation "
+                                     "bits + 2 diagonal-energy features of the string under its Hamiltonian) -> 3 x 256 "
                                      "GELU -> (log|a|, phase), BF16 tensor-core training on the post-selected ground "
                                      "projections of 512 seeded Hamiltonians (QPE with 6 ancilla qubits, complex64), "
                                      "evaluated on 64 held-out seeds against Hartree-Fock")
@@ -652,18 +653,20 @@ def run_learned(args, w, rank, ws, local):
     timer = N.Timer(local)
 
     def programs(seeds):
-        out = []
+        """Programs of the seeds' Hamiltonians and the model's features of every string under each."""
+        out, feats = [], []
         for s in seeds:
             h = q.Hamiltonian.from_integrals(q.synthetic_integrals(w["n"], s), na, dt)
             out.append(q.Program(h.segmented_terms(), M, na, nb, device=local))
-        return out
+            feats.append(L.diagonal_features(h, strings))
+        return out, feats
 
     base = w["seed"] + 100000 * rank
     train_seeds = [base + i for i in range(w["train"])]
     eval_seeds = [base + 50000 + i for i in range(w["held_out"])]
     t0 = time.perf_counter()
     # 1. post-selected ground projections of the training Hamiltonians
-    progs = programs(train_seeds)
+    progs, tfeats = programs(train_seeds)
     bt = q.Batch(progs, Pd, dtype=np.complex64, device=local)
     hf = q.hf_block0(math.comb(M, na), math.comb(M, nb), Pd, np.complex64)
     for i in range(len(progs)):
@@ -686,29 +689,28 @@ def run_learned(args, w, rank, ws, local):
     del bt, progs
     data_s = time.perf_counter() - t0
     # 2. training on the tensor cores
-    model = L.AmplitudeMLP(w["n"], batch=w["batch"], seed=w["seed"], device=local)
-    model.set_data(np.concatenate(bits), np.concatenate(la), np.concatenate(ph), np.concatenate(wt))
+    model = L.AmplitudeMLP(w["n"], batch=w["batch"], seed=w["seed"], device=local, n_feat=L.N_DIAG_FEATURES)
+    model.set_data(np.concatenate(bits), np.concatenate(la), np.concatenate(ph), np.concatenate(wt),
+                   np.concatenate(tfeats))
     model.train(20, lr=w["lr"], seed=1)  # warm-up
     t1 = time.perf_counter()
     losses = model.train(w["train_steps"], lr=w["lr"], seed=2)
     train_s = time.perf_counter() - t1
     tflops = model.tensor_flops_per_step() * w["train_steps"] / train_s / 1e12
     # 3. evaluation: QPE from HF and from the learned state on held-out Hamiltonians
-    eprogs = programs(eval_seeds)
+    eprogs, efeats = programs(eval_seeds)
     bt = q.Batch(eprogs + eprogs, P, dtype=np.complex64, device=local)
     hfP = q.hf_block0(math.comb(M, na), math.comb(M, nb), P, np.complex64)
     scale = 2.0 ** (-P / 2)
-    learned_states = []
+    # the model's state for each held-out Hamiltonian (its features differ per Hamiltonian)
+    learned_states = [L.proposed_state(model, strings, efeats[i]) for i in range(len(eprogs))]
     for i in range(len(eprogs)):
         bt.upload(i, hfP)
-        # the same model for every Hamiltonian: its state does not depend on i
-        if not learned_states:
-            learned_states.append(L.proposed_state(model, strings))
-        bt.upload(len(eprogs) + i, (learned_states[0] * scale).astype(np.complex64))
+        bt.upload(len(eprogs) + i, (learned_states[i] * scale).astype(np.complex64))
     bt.run()  # warm-up of the graph
     for i in range(len(eprogs)):
         bt.upload(i, hfP)
-        bt.upload(len(eprogs) + i, (learned_states[0] * scale).astype(np.complex64))
+        bt.upload(len(eprogs) + i, (learned_states[i] * scale).astype(np.complex64))
     timer.record(2)
     bt.run()
     timer.record(3)
@@ -724,7 +726,7 @@ def run_learned(args, w, rank, ws, local):
         psi_hf = np.zeros(ld, np.complex128)
         psi_hf[0] = 1.0
         ov_hf = float(abs(np.vdot(g, psi_hf)) ** 2)
-        ov_l = float(abs(np.vdot(g, learned_states[0])) ** 2)
+        ov_l = float(abs(np.vdot(g, learned_states[i])) ** 2)
         s_hf, s_l = L.window_mass(p_hf, j0), L.window_mass(p_l, j0)
         n_hf = L.shots_to_precision(p_hf, j0, dt, e_t, seed=i)
         n_l = L.shots_to_precision(p_l, j0, dt, e_t, seed=i)

@@ -27,6 +27,11 @@ typedef struct qpe_mlp qpe_mlp;
 /* A model with seeded initial weights; `batch` (a multiple of 128) is the number
  * of samples per training step and per forward chunk. */
 int qpe_mlp_create(qpe_context* ctx, uint32_t n_bits, uint32_t batch, uint64_t seed, qpe_mlp** out);
+/* The same with n_feat extra real input features per sample after the n_bits
+ * occupations (n_bits + n_feat <= 64), e.g. quantities of the Hamiltonian the
+ * string belongs to; the *2 calls below then take them, n_feat floats per sample. */
+int qpe_mlp_create2(qpe_context* ctx, uint32_t n_bits, uint32_t n_feat, uint32_t batch, uint64_t seed,
+                    qpe_mlp** out);
 int qpe_mlp_destroy(qpe_mlp* m);
 
 /* Parameters as one FP32 array, in this order: W1 [256 x 64] (input columns past
@@ -40,6 +45,8 @@ int qpe_mlp_set_params(qpe_mlp* m, const float* host);
  * target log|a|, phase, and the loss weight. */
 int qpe_mlp_set_data(qpe_mlp* m, const uint64_t* bits, const float* log_abs, const float* phase,
                      const float* weight, uint64_t count);
+int qpe_mlp_set_data2(qpe_mlp* m, const uint64_t* bits, const float* feats, const float* log_abs, const float* phase,
+                      const float* weight, uint64_t count);
 
 /* `steps` Adam steps (learning rate lr) on batches drawn from the training set
  * with a seeded hash; losses (may be NULL) receives each step's loss:
@@ -48,11 +55,14 @@ int qpe_mlp_train(qpe_mlp* m, uint32_t steps, float lr, uint64_t seed, float* lo
 
 /* Model outputs for `count` strings: out[2 i] = log|a|, out[2 i + 1] = phase. */
 int qpe_mlp_forward(qpe_mlp* m, const uint64_t* bits, uint64_t count, float* out);
+int qpe_mlp_forward2(qpe_mlp* m, const uint64_t* bits, const float* feats, uint64_t count, float* out);
 
 /* Loss and gradient of every parameter (the qpe_mlp_get_params layout) on one
  * batch of `count` <= batch samples, without an update. */
 int qpe_mlp_gradients(qpe_mlp* m, const uint64_t* bits, const float* log_abs, const float* phase,
                       const float* weight, uint32_t count, float* grads, float* loss);
+int qpe_mlp_gradients2(qpe_mlp* m, const uint64_t* bits, const float* feats, const float* log_abs,
+                       const float* phase, const float* weight, uint32_t count, float* grads, float* loss);
 
 /* Tensor-core FLOPs of one training step (the 11 GEMMs). */
 int qpe_mlp_tensor_flops_per_step(const qpe_mlp* m, double* flops);

@@ -109,3 +109,17 @@ def test_qpe_energy_on_the_spectrum(q, orc):
     # and the first-order Trotter shift
     res = 2 * math.pi / (dt * (1 << P))
     assert np.min(np.abs(evals - est)) < 0.5 * res + 0.05
+
+
+def test_diagonal_energies_match_the_sector_hamiltonian(q, orc):
+    """The learned model's diagonal-energy feature <x|H|x> (pp and pqqp terms) is
+    the diagonal of the sector Hamiltonian read back from the sweep."""
+    M, e = 4, 2
+    ints = q.synthetic_integrals(8, 3)
+    H, _ = _sector_hamiltonian(q, orc, M, e, ints)
+    h = q.Hamiltonian.from_integrals(ints, e, 0.05)
+    L = q.learned_state
+    strings = L.register_strings(M, e, e)
+    assert np.abs(L.diagonal_energies(h, strings) - np.diag(H)).max() < 1e-12
+    f = L.diagonal_features(h, strings)
+    assert f.shape == (len(strings), L.N_DIAG_FEATURES) and f[:, 0].min() == 0.0 and f[:, 1].max() == 1.0

@@ -45,8 +45,9 @@ def _gelu_grad(x):
     return 0.5 * (1 + erf(x / math.sqrt(2))) + x * np.exp(-0.5 * x * x) / math.sqrt(2 * math.pi)
 
 
-def _reference(ls, p, bits, n_bits, tla, tph, w):
-    """FP64 forward / backward with BF16 rounding where the device rounds."""
+def _reference(ls, p, bits, n_bits, tla, tph, w, feats=None):
+    """FP64 forward / backward with BF16 rounding where the device rounds (the
+    extra input features, if any, are rounded to BF16 like the rest of X0)."""
     lay = ls.param_layout()
     P = {k: p[o:o + int(np.prod(s))].reshape(s).astype(np.float64) for k, (o, s) in lay.items()}
     rb = lambda x: ls.round_bf16(np.asarray(x, np.float32)).astype(np.float64)  # noqa: E731
@@ -55,6 +56,8 @@ def _reference(ls, p, bits, n_bits, tla, tph, w):
     X0 = np.zeros((B, 64))
     for j in range(n_bits):
         X0[:, j] = (bits >> np.uint64(j)) & np.uint64(1)
+    if feats is not None:
+        X0[:, n_bits:n_bits + feats.shape[1]] = rb(feats)
     Z1 = X0 @ W["W1"].T + P["b1"]
     H1 = rb(_gelu(Z1))
     Z2 = H1 @ W["W2"].T + P["b2"]
@@ -75,9 +78,13 @@ def _reference(ls, p, bits, n_bits, tla, tph, w):
     return Y[:, :2], loss, g
 
 
-def test_mlp_forward_and_gradients_against_fp64(ls):
+@pytest.mark.parametrize("n_feat", [0, 2])
+def test_mlp_forward_and_gradients_against_fp64(ls, n_feat):
+    """Outputs, loss and every parameter gradient against the FP64 restatement;
+    with n_feat > 0 the model also takes per-sample real features after the
+    occupation bits."""
     n_bits, B = 20, 384
-    m = ls.AmplitudeMLP(n_bits, batch=512, seed=3)
+    m = ls.AmplitudeMLP(n_bits, batch=512, seed=3, n_feat=n_feat)
     rng = np.random.default_rng(5)
     p = m.get_params()
     lay = ls.param_layout()
@@ -90,11 +97,12 @@ def test_mlp_forward_and_gradients_against_fp64(ls):
     tla = rng.standard_normal(B).astype(np.float32)
     tph = rng.uniform(-3, 3, B).astype(np.float32)
     w = rng.uniform(0.2, 2.0, B).astype(np.float32)
+    feats = rng.uniform(-2, 2, (B, n_feat)).astype(np.float32) if n_feat else None
     y_ref, loss_ref, g_ref = _reference(ls, p, bits, n_bits, tla.astype(np.float64), tph.astype(np.float64),
-                                        w.astype(np.float64))
-    y = m.forward(bits)
+                                        w.astype(np.float64), feats)
+    y = m.forward(bits, feats)
     np.testing.assert_allclose(y, y_ref, rtol=0, atol=2e-2 * np.abs(y_ref).max())
-    g, loss = m.gradients(bits, tla, tph, w)
+    g, loss = m.gradients(bits, tla, tph, w, feats)
     assert abs(loss - loss_ref) <= 1e-2 * abs(loss_ref)
     for k, (o, s) in lay.items():
         got = g[o:o + int(np.prod(s))].reshape(s).astype(np.float64)
@@ -109,7 +117,7 @@ def test_mlp_forward_and_gradients_against_fp64(ls):
         assert err < 5e-3, (k, err)
     # padding stays exactly zero
     o, s = lay["W1"]
-    assert not np.any(g[o:o + 256 * 64].reshape(256, 64)[:, n_bits:])
+    assert not np.any(g[o:o + 256 * 64].reshape(256, 64)[:, n_bits + n_feat:])
 
 
 def test_mlp_training_fits_a_smooth_target(ls):
