@@ -3,6 +3,7 @@
  *
  * An MLP over occupation bit strings proposes the amplitudes of the QPE initial
  * state in place of Hartree-Fock: n_bits inputs (bit j of the string as 0 / 1),
+ * optionally followed by n_feat real features of the string (qpe_mlp_create2),
  * three hidden layers of 256 with GELU, outputs (log|a|, phase). BF16 weights and
  * activations with FP32 accumulation on the tensor cores (tcgen05 MMA, TMA
  * operand loads); FP32 master weights, Adam moments and loss.
