@@ -16,6 +16,7 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "lib" / "libqpe_gb300.so"
 
 QPE_OK = 0
+QPE_ERR_INVALID, QPE_ERR_UNSUPPORTED, QPE_ERR_NOMEM, QPE_ERR_CUDA, QPE_ERR_TIMEOUT, QPE_ERR_NO_DEVICE = 1, 2, 3, 4, 5, 6
 ERRORS = {1: "invalid argument", 2: "unsupported", 3: "out of memory", 4: "CUDA error", 5: "timeout",
           6: "no CUDA device"}
 QPE_C128, QPE_C64 = 0, 1
@@ -71,6 +72,8 @@ PROTOTYPES = {
     "qpe_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_vp)]),
     "qpe_host_free": (C.c_int, [_vp]),
     "qpe_flush_l2": (C.c_int, [_vp]),
+    "qpe_measure_fp64_peak": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "qpe_selftest_bounded_wait": (C.c_int, [_vp, C.c_uint32, C.c_int]),
     "qpe_rank": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_int64), C.c_size_t]),
     "qpe_unrank": (C.c_int, [_vp, C.c_uint32, C.c_uint32, C.POINTER(C.c_int64), C.POINTER(C.c_uint64), C.c_size_t]),
     "qpe_rank_with_swaps": (C.c_int, [_vp, C.c_uint32, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_int64),

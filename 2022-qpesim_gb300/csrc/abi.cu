@@ -67,8 +67,9 @@ void qift_geometry(uint32_t P, uint64_t ld, int dtype, int num_sms, size_t smem_
   grid = (uint32_t)g;
 }
 
-// Twiddles exp(-2 pi i k / N), k < N / 2, rounded from long double (as the oracle).
-void state_twiddles(uint32_t P, int dtype, DevBuf& tw) {
+// Twiddles exp(-2 pi i k / N), k < N / 2 (at least one), rounded from long double
+// (as the oracle), interleaved (re, im).
+std::vector<double> twiddle_table(uint32_t P) {
   const uint64_t N = 1ull << P;
   const uint64_t nh = N / 2 ? N / 2 : 1;
   std::vector<double> twd(2 * nh);
@@ -78,6 +79,11 @@ void state_twiddles(uint32_t P, int dtype, DevBuf& tw) {
     twd[2 * k] = (double)cosl(ang);
     twd[2 * k + 1] = (double)sinl(ang);
   }
+  return twd;
+}
+
+void state_twiddles(uint32_t P, int dtype, DevBuf& tw) {
+  const std::vector<double> twd = twiddle_table(P);
   if (dtype == QPE_C128) {
     tw.alloc(twd.size() * sizeof(double));
     QPE_CK(cudaMemcpy(tw.p, twd.data(), twd.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -673,6 +679,26 @@ int qpe_flush_l2(qpe_context* ctx) {
     check_ctx(ctx);
     if (!ctx->flush.p) ctx->flush.alloc(256ull << 20);
     QPE_CK(cudaMemsetAsync(ctx->flush.p, 0x5a, ctx->flush.bytes, ctx->stream));
+  });
+}
+
+int qpe_measure_fp64_peak(qpe_context* ctx, double* tflops) {
+  return guard([&] {
+    check_ctx(ctx);
+    if (!tflops) throw Error(QPE_ERR_INVALID, "null output");
+    DevBuf out;
+    const uint32_t ctas = (uint32_t)ctx->num_sms * 4, threads = 256, iters = 4096;
+    out.alloc((size_t)ctas * threads * sizeof(double));
+    QPE_CK(launch_fp64_fma_probe(out.as<double>(), ctas, threads, iters, ctx->stream));  // warm-up
+    QPE_CK(cudaEventRecord(ctx->events[14], ctx->stream));
+    const int reps = 4;
+    for (int r = 0; r < reps; ++r) QPE_CK(launch_fp64_fma_probe(out.as<double>(), ctas, threads, iters, ctx->stream));
+    QPE_CK(cudaEventRecord(ctx->events[15], ctx->stream));
+    QPE_CK(cudaEventSynchronize(ctx->events[15]));
+    float ms = 0.f;
+    QPE_CK(cudaEventElapsedTime(&ms, ctx->events[14], ctx->events[15]));
+    const double flops = 2.0 * kFp64ProbeChains * (double)iters * ctas * threads * reps;
+    *tflops = flops / (ms * 1e-3) / 1e12;
   });
 }
 

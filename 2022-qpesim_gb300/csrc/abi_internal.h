@@ -74,6 +74,7 @@ struct qpe_program {
 namespace qpe {
 // Launch geometry of one pass of `pr` for elements of esz bytes.
 PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_optin, const Pass& pass);
+std::vector<double> twiddle_table(uint32_t P);
 void state_twiddles(uint32_t P, int dtype, DevBuf& tw);
 void qift_geometry(uint32_t P, uint64_t ld, int dtype, int num_sms, size_t smem_optin, uint32_t& T, uint32_t& grid);
 }  // namespace qpe

@@ -309,4 +309,27 @@ cudaError_t launch_build_tables(const uint64_t* d_binom, const AxisTable* d_tabs
   return cudaGetLastError();
 }
 
+// FP64 FMA throughput probe: kFp64ProbeChains independent FMA chains per
+// thread, `iters` steps each, the chains' sum stored so that nothing is dropped.
+__global__ void k_fp64_fma_probe(double* __restrict__ out, uint32_t iters) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  double a[kFp64ProbeChains];
+#pragma unroll
+  for (int c = 0; c < kFp64ProbeChains; ++c) a[c] = 1.0 + 1e-9 * (tid + c);
+  const double m = 0.999999999, k = 1e-12;
+  for (uint32_t i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < kFp64ProbeChains; ++c) a[c] = fma(a[c], m, k);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < kFp64ProbeChains; ++c) s += a[c];
+  out[tid] = s;
+}
+
+cudaError_t launch_fp64_fma_probe(double* out, uint32_t ctas, uint32_t threads, uint32_t iters, cudaStream_t s) {
+  k_fp64_fma_probe<<<ctas, threads, 0, s>>>(out, iters);
+  return cudaGetLastError();
+}
+
 }  // namespace qpe

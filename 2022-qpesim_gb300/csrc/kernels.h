@@ -26,6 +26,11 @@ cudaError_t launch_line_strings(const uint64_t* d_binom, uint32_t nbits, uint32_
 cudaError_t launch_build_tables(const uint64_t* d_binom, const AxisTable* d_tabs, const uint32_t* d_entry_start,
                                 uint32_t ntabs, uint64_t total_entries, uint32_t* d_pool, cudaStream_t s);
 
+// FP64 FMA throughput probe (qpe_measure_fp64_peak): ctas x threads threads,
+// kFp64ProbeChains independent FMA chains of `iters` steps each.
+constexpr int kFp64ProbeChains = 8;
+cudaError_t launch_fp64_fma_probe(double* out, uint32_t ctas, uint32_t threads, uint32_t iters, cudaStream_t s);
+
 // ---- evolution (evolve.cu) ----
 struct PassLaunch {
   void* work;                 // working block (Ca x Cb complex)

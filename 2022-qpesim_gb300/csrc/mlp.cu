@@ -650,6 +650,23 @@ static void check_err(qpe_mlp* m) {
   if (e) throw Error(QPE_ERR_TIMEOUT, "tensor-core GEMM: a pipeline wait ran out (code " + std::to_string(e) + ")");
 }
 
+// The bounded wait every tcgen05 / TMA pipeline wait of this file uses
+// (umma::mbar_wait), run alone on one mbarrier with nothing in flight: thread 0
+// initialises it for one arrival and, if `arrive`, arrives; then every thread
+// waits for phase 0 with `max_tries` polls. A wait that runs out sets *err and
+// the kernel returns, as the GEMM kernels do.
+__global__ void k_wait_probe(uint32_t max_tries, int arrive, int* err) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t b = umma::smem_u32(&bar);
+  if (threadIdx.x == 0) {
+    umma::mbar_init(b, 1);
+    umma::fence_barrier_init();
+  }
+  __syncthreads();
+  if (arrive && threadIdx.x == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(b) : "memory");
+  if (!umma::mbar_wait(b, 0, max_tries)) atomicOr(err, 1);
+}
+
 static void use_ctx(qpe_context* ctx) {
   if (!ctx) throw Error(QPE_ERR_INVALID, "null context");
   QPE_CK(cudaSetDevice(ctx->device));
@@ -917,6 +934,24 @@ int qpe_gemm_bf16(qpe_context* ctx, uint32_t M, uint32_t N, uint32_t K, const ui
     QPE_CK(cudaMemcpy(&err, e.p, 4, cudaMemcpyDeviceToHost));
     if (err) throw Error(QPE_ERR_TIMEOUT, "tensor-core GEMM: a pipeline wait ran out");
     QPE_CK(cudaMemcpy(D, dD.p, (size_t)M * N * 4, cudaMemcpyDeviceToHost));
+  });
+}
+
+int qpe_selftest_bounded_wait(qpe_context* ctx, uint32_t max_tries, int arrive) {
+  return guard([&] {
+    use_ctx(ctx);
+    if (max_tries == 0) throw Error(QPE_ERR_INVALID, "max_tries must be positive");
+    DevBuf e;
+    e.alloc(16);
+    QPE_CK(cudaMemsetAsync(e.p, 0, 16, ctx->stream));
+    k_wait_probe<<<1, 32, 0, ctx->stream>>>(max_tries, arrive ? 1 : 0, e.as<int>());
+    QPE_CK(cudaGetLastError());
+    int err = 0;
+    QPE_CK(cudaMemcpyAsync(&err, e.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    QPE_CK(cudaStreamSynchronize(ctx->stream));
+    if (err)
+      throw Error(QPE_ERR_TIMEOUT, "bounded device wait ran out after " + std::to_string(max_tries) +
+                                       " polls (mbarrier never completed); the kernel returned and the context is usable");
   });
 }
 

@@ -34,7 +34,21 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 import __graft_entry__ as graft  # noqa: E402
 
-FP64_PEAK_TFLOPS = 1.19  # measured FP64 FMA throughput of this GB300 (own probe; not in MEASURED_PEAKS.json)
+
+
+def load_synthetic():
+    """The workloads' integral generator (2022-qpesim_gb300/synthetic.py, numpy
+    only), loaded from its file on its own, so that the reference arm draws the
+    same integrals without importing the package or loading its library."""
+    name = "qpe_workload_synthetic"
+    mod = sys.modules.get(name)
+    if mod is None:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location(name, ROOT / "2022-qpesim_gb300" / "synthetic.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return mod
 
 WORKLOADS = {
     # Plain QPE in FP64: n = 16, N = 8, 10 ancilla qubits (the default workload).
@@ -97,6 +111,67 @@ def peaks():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+DATA_NOTE = ("synthetic: seeded integrals (h_pq ~ N(0,1) exp(-|p-q|/2), (pq|rs) ~ N(0,0.1^2) "
+             "exp(-(|p-q|+|r-s|)/3)), Hartree-Fock start, one replica per rank")
+
+
+def workload_config(args, w, touches_per_power, ws):
+    """The `config` object of a single-instance workload, identical in both arms."""
+    M, na, P = w["n"] // 2, w["N"] // 2, w["P"]
+    npow = (1 << P) - 1
+    if getattr(args, "powers", 0):
+        npow = min(npow, args.powers)
+    cfg = {"workload": args.workload, "description": w["desc"], "n_spin_orbitals": w["n"], "electrons": w["N"],
+           "precision": P, "dt": w["dt"], "trotter_order": w["order"], "steps_per_power": w["steps"],
+           "state": w["dtype"], "amps_per_block": math.comb(M, na) ** 2, "blocks": 1 << P,
+           "touches_per_power": int(touches_per_power), "touches_per_step": int(touches_per_power) * npow,
+           "l2": "flushed before every timed step (256 MiB write)", "parallelism": f"replicas x{ws}"}
+    if getattr(args, "powers", 0):
+        cfg["powers_evolved"] = npow
+    if getattr(args, "precision", 0):
+        cfg["precision_override"] = args.precision
+    return cfg
+
+
+def measure_fp64_peak(N, ctx):
+    """The device's FP64 FMA throughput in TFLOP/s, measured live by the library's
+    probe (qpe_measure_fp64_peak: 8 independent FMA chains per thread, 4 CTAs of
+    256 threads per SM, CUDA events)."""
+    import ctypes
+    v = ctypes.c_double()
+    N.check(N.lib().qpe_measure_fp64_peak(ctx, ctypes.byref(v)))
+    return v.value
+
+
+def roofline_single(w, achieved, peak, peak_kind, kernel, touches_step, ev_s, fp64_peak):
+    """Roofline object of a single-instance workload. achieved is the algorithmic
+    HBM figure (2 * sizeof(amplitude) per touch over the evolution time); `bound`
+    names the resource that limits the dominant kernel, as measured."""
+    r = {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+         "peak_source": peak_kind, "peak_note": f"{peak_kind} HBM copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
+         "kernel": kernel}
+    if w["dtype"] == "c128":
+        ops = touches_step * 6 / ev_s / 1e12  # 6 FP64 DMUL / DADD per touch, no FMA (reference rounding)
+        r["bound"] = "latency"
+        r["bound_note"] = ("pass latency: every controlled power is a chain of dependent passes (a cluster "
+                           "barrier each) whose terms are chains of dependent FP64 operations on one block "
+                           "held in the cluster's shared memory; DRAM moves only the snapshots (traffic below), "
+                           "and FP64 issue is a small fraction of the live-measured peak (fp64)")
+        r["fp64"] = {"achieved_tflops": ops, "peak_fma_tflops": fp64_peak,
+                     "frac_of_fma_peak": ops / fp64_peak if fp64_peak else None,
+                     "frac_of_issue_rate": 2 * ops / fp64_peak if fp64_peak else None,
+                     "ops_per_touch": 6,
+                     "peak_method": "measured live in this run by qpe_measure_fp64_peak (an FMA counts 2 FLOP; "
+                                    "the path issues DMUL and DADD, so its ceiling is half the FMA FLOP/s: "
+                                    "frac_of_issue_rate)"}
+    else:
+        r["bound"] = "latency"
+        r["bound_note"] = ("L2 latency: the complex64 working block stays in L2 across the passes, so the "
+                           "tile passes wait on L2 round trips; the algorithmic HBM figure is a ceiling "
+                           "reference, not the binding resource")
+    return r
 
 
 class Clocks:
@@ -190,35 +265,60 @@ def build_problem(q, w, seed_offset=0):
     return h, h.segmented_terms()
 
 
-def cpu_baseline(q, w, seg, budget_s=15.0, fast=True):
-    """The oracle (CPU restatement of the reference) on a bounded sample: as many
-    controlled powers as fit in about budget_s, with the better of 1 thread and
-    all host threads. Returns (touches/s, threads, sample description)."""
-    O = graft.load_oracle()
-    orc = O.Oracle(fast=fast)
+def oracle_terms(orc, w, n, n_alpha, seed):
+    """The workload's segmented terms from the oracle's own term compiler (the
+    reference's, restated in oracle/terms_oracle.cc): seeded synthetic integrals,
+    coefficients at dt (first order) or dt / 2 (each sweep of a second-order step)."""
+    ints = load_synthetic().synthetic_integrals(n, seed)
+    t = w["dt"] / 2 if w["order"] == 2 else w["dt"]
+    return orc.segmented_terms(n // 2, n_alpha, t, ints.one_body, ints.two_body)
+
+
+def thread_choices():
+    n = os.cpu_count() or 1
+    return sorted({1, 2, 4, 8, n} & set(range(1, n + 1)))
+
+
+def choose_threads(orc, run_powers, trial_powers=2):
+    """The host thread count the CPU evolution runs fastest with: every count in
+    thread_choices() times `trial_powers` controlled powers (run_powers(k) evolves
+    k powers); returns (threads, seconds per power at that count)."""
+    best = None
+    for th in thread_choices():
+        orc.set_threads(th)
+        t0 = time.perf_counter()
+        run_powers(trial_powers)
+        per = (time.perf_counter() - t0) / trial_powers
+        if best is None or per < best[1]:
+            best = (th, per)
+    orc.set_threads(best[0])
+    return best
+
+
+def cpu_baseline(orc, w, seg, budget_s=15.0):
+    """The oracle (CPU restatement of the reference, liborc_fast.so) on a bounded
+    sample of the workload: as many controlled powers as fit in about budget_s,
+    at the fastest host thread count. Returns (touches/s, threads, sample dict)."""
     M, e, P = w["n"] // 2, w["N"] // 2, w["P"]
     C2 = math.comb(M, e) ** 2
-    prog_touches = q.plan_program(seg, M, e, e, w["order"], w["steps"])["touches_per_power"]
+    touches = orc.touches_per_power(M, e, e, seg, w["order"], w["steps"])
+    total = (1 << P) - 1
     state = np.zeros((1 << P) * C2, np.complex128)
     state[0] = 2 ** (-P / 2)
-    ncpu = os.cpu_count() or 1
-    best = None
-    for threads in sorted({1, ncpu}):
-        orc.set_threads(threads)
-        t0 = time.perf_counter()
-        orc.time_evolve(M, e, e, P, seg, state, order=w["order"], steps=w["steps"], first=1, last=2)
-        dt1 = time.perf_counter() - t0
-        if best is None or dt1 < best[1]:
-            best = (threads, dt1)
-    threads, per_power = best
-    orc.set_threads(threads)
-    npow = int(max(1, min((1 << P) - 1, budget_s / max(per_power, 1e-9))))
+
+    def run_powers(k):
+        orc.time_evolve(M, e, e, P, seg, state, order=w["order"], steps=w["steps"], first=1, last=1 + k)
+
+    threads, per_power = choose_threads(orc, run_powers)
+    npow = int(max(1, min(total, budget_s / max(per_power, 1e-9))))
     t0 = time.perf_counter()
-    orc.time_evolve(M, e, e, P, seg, state, order=w["order"], steps=w["steps"], first=1, last=1 + npow)
+    run_powers(npow)
     el = time.perf_counter() - t0
-    rate = prog_touches * npow / el
-    return rate, threads, (f"{npow} of {(1 << P) - 1} controlled powers of the same workload "
-                           f"({el:.1f} s, {threads} thread(s)); QIFT excluded")
+    return touches * npow / el, threads, {
+        "powers_sampled": npow, "powers_total": total, "seconds": el, "threads": threads,
+        "thread_choices": thread_choices(), "touches_per_power": touches,
+        "what": f"{npow} of {total} controlled powers of the same workload from the Hartree-Fock start "
+                f"({el:.1f} s, {threads} thread(s), fastest of {thread_choices()}); QIFT excluded"}
 
 
 def run_ours(args, w, rank, ws, local):
@@ -299,6 +399,7 @@ def run_ours(args, w, rank, ws, local):
     peak, peak_kind = peaks()
     info = prog.info
     strat, kc = st.last_strategy()
+    fp64_peak = measure_fp64_peak(N, ctx) if w["dtype"] == "c128" else None
     if strat == 3:
         kernel = "k_pass (evolution tile passes, one launch per pass)"
         launches = args.steps * (npow * (info["num_passes_per_power"] + 2) + 1 + 2 + 1)
@@ -323,46 +424,26 @@ def run_ours(args, w, rank, ws, local):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64" if w["dtype"] == "c128" else "f32",
-        "data": "synthetic: seeded integrals (h_pq ~ N(0,1) exp(-|p-q|/2), (pq|rs) ~ N(0,0.1^2) "
-                "exp(-(|p-q|+|r-s|)/3)), one replica per rank",
-        "config": {"workload": args.workload, "description": w["desc"], "n_spin_orbitals": w["n"],
-                   "electrons": w["N"], "precision": P, "dt": w["dt"], "trotter_order": w["order"],
-                   "steps_per_power": w["steps"], "state": w["dtype"], "amps_per_block": st.ld,
-                   "blocks": 1 << P, "touches_per_power": prog.touches_per_power,
-                   "touches_per_step": touches_step, "l2": "flushed before every timed step",
-                   "parallelism": f"replicas x{ws}", "strategy": strategy_name},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
-                     "kernel": kernel,
-                     # 6 FP64 operations (DMUL / DADD, no FMA in exact mode) per touch, against the
-                     # FP64 issue rate: half the FMA FLOP/s, one operation per lane per issue
-                     "fp64": {"achieved_tops": touches_step * 6 / ev_s / 1e12, "peak_tops": FP64_PEAK_TFLOPS / 2,
-                              "frac": touches_step * 6 / ev_s / 1e12 / (FP64_PEAK_TFLOPS / 2),
-                              "ops_per_touch": 6,
-                              "note": "one controlled power is a chain of 3,200 dependent passes on the 16 SMs "
-                                      "of one cluster; a pass's terms are chains of dependent FP64 operations "
-                                      "(64 cycles of issue per warp instruction), so the bound is the chain's "
-                                      "latency, not throughput"}} if w["dtype"] == "c128" else
-                    {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": peak_kind, "kernel": kernel},
+        "data": DATA_NOTE,
+        "config": workload_config(args, w, prog.touches_per_power, ws),
+        "kernel_strategy": strategy_name,
+        "roofline": roofline_single(w, achieved, peak, peak_kind, kernel, touches_step, ev_s, fp64_peak),
         "e2e": {"value": e2e_value, "unit": "touches/s",
                 "h2d_bytes_per_step": int(st.ld * dtype().itemsize),
                 "d2h_bytes_per_step": int(st.size * dtype().itemsize + (1 << P) * 8)},
         "gpu_launches": launches,
         "clocks": clk,
     }
-    if args.powers:
-        line["config"]["powers_evolved"] = npow
-    if args.precision:
-        line["config"]["precision_override"] = args.precision
     if args.workload in MEASURED_TRAFFIC:
         line["roofline"]["traffic"], line["roofline"]["traffic_note"] = MEASURED_TRAFFIC[args.workload]
     if w.get("check_c128") and not args.powers:
         line["precision_check"] = precision_check(q, w, seg, st, prog, block0, local)
     if rank == 0 and not args.no_cpu_baseline:
-        rate, threads, sample = cpu_baseline(q, w, seg)
+        orc = graft.load_oracle().Oracle(fast=True)
+        rate, threads, sample = cpu_baseline(orc, w, seg)
         line["cpu_baseline"] = {"value": rate, "unit": "touches/s", "cores": threads, "kind": "port",
-                                "sample": sample}
+                                "sample": sample["what"], "powers_sampled": sample["powers_sampled"],
+                                "powers_total": sample["powers_total"]}
     return line
 
 
@@ -407,6 +488,8 @@ def batch_instances(w, rank=0):
 
 
 def build_batch_terms(q, w, rank=0):
+    """(n, n_alpha, n_beta, segmented terms) of every instance, from the package's
+    term compiler (the GPU arm)."""
     out = []
     for n, Nel, seed in batch_instances(w, rank):
         h = q.Hamiltonian.from_integrals(q.synthetic_integrals(n, seed), (Nel + 1) // 2, w["dt"])
@@ -414,47 +497,68 @@ def build_batch_terms(q, w, rank=0):
     return out
 
 
-def cpu_baseline_batch(q, w, terms, budget_s=20.0):
+def build_batch_terms_oracle(orc, w, rank=0):
+    """The same instances' terms from the oracle's own term compiler (the
+    reference arm; bit-identical to the package's)."""
+    return [(n, (Nel + 1) // 2, Nel // 2, oracle_terms(orc, w, n, (Nel + 1) // 2, seed))
+            for n, Nel, seed in batch_instances(w, rank)]
+
+
+def batch_config(args, w, terms, touches_per_step, ws):
+    """The `config` object of a batched workload, identical in both arms."""
+    sizes = {}
+    for n, *_ in terms:
+        sizes[str(n)] = sizes.get(str(n), 0) + 1
+    return {"workload": args.workload, "description": w["desc"], "instances": len(terms),
+            "instances_per_n": dict(sorted(sizes.items(), key=lambda kv: int(kv[0]))), "precision": w["P"],
+            "dt": w["dt"], "trotter_order": w["order"], "steps_per_power": w["steps"], "state": w["dtype"],
+            "touches_per_step": int(touches_per_step), "l2": "flushed before every timed step (256 MiB write)",
+            "parallelism": f"replicas x{ws}"}
+
+
+def cpu_baseline_batch(orc, w, terms, budget_s=20.0):
     """The oracle on a bounded sample of the batch: one instance of each size, the
-    powers that fit in its share of the budget, the better of 1 thread and all
-    host threads per size; the batch's CPU time is the sum over its instances at
-    those per-size rates."""
-    O = graft.load_oracle()
-    orc = O.Oracle(fast=True)
+    powers that fit in its share of the budget at its fastest host thread count;
+    the batch's CPU time is the sum over its instances at those per-size rates.
+    Returns (touches/s, max threads used, sample dict)."""
     P = w["P"]
-    ncpu = os.cpu_count() or 1
+    total = (1 << P) - 1
     rate, cores, parts = {}, {}, []
     sizes = sorted({t[0] for t in terms})
+    touches_of = {}
+    for n, na, nb, seg in terms:
+        key = (n, na, nb, id(seg))
+        touches_of[key] = orc.touches_per_power(n // 2, na, nb, seg, w["order"], w["steps"])
+    sampled = 0
     for n in sizes:
         n_, na, nb, seg = next(t for t in terms if t[0] == n)
         M = n // 2
-        touches = q.plan_program(seg, M, na, nb, w["order"], w["steps"])["touches_per_power"]
+        touches = touches_of[(n_, na, nb, id(seg))]
         ld = math.comb(M, na) * math.comb(M, nb)
         state = np.zeros((1 << P) * ld, np.complex128)
         state[0] = 2 ** (-P / 2)
-        best = None
-        for threads in sorted({1, ncpu}):
-            orc.set_threads(threads)
-            t0 = time.perf_counter()
-            orc.time_evolve(M, na, nb, P, seg, state, first=1, last=2)
-            el = time.perf_counter() - t0
-            if best is None or el < best[1]:
-                best = (threads, el)
-        orc.set_threads(best[0])
-        npow = int(max(1, min((1 << P) - 1, budget_s / len(sizes) / max(best[1], 1e-9))))
+
+        def run_powers(k):
+            orc.time_evolve(M, na, nb, P, seg, state, order=w["order"], steps=w["steps"], first=1, last=1 + k)
+
+        th, per = choose_threads(orc, run_powers, trial_powers=1)
+        npow = int(max(1, min(total, budget_s / len(sizes) / max(per, 1e-9))))
         t0 = time.perf_counter()
-        orc.time_evolve(M, na, nb, P, seg, state, first=1, last=1 + npow)
+        run_powers(npow)
         el = time.perf_counter() - t0
         rate[n] = touches * npow / el
-        cores[n] = best[0]
-        parts.append(f"n={n}: {npow} powers, {best[0]} thread(s), {rate[n] / 1e6:.0f} M/s")
-    total_t = 0.0
-    total_touch = 0
+        cores[n] = th
+        sampled += npow
+        parts.append(f"n={n}: {npow} powers, {th} thread(s), {rate[n] / 1e6:.0f} M/s")
+    total_t, total_touch = 0.0, 0
     for n, na, nb, seg in terms:
-        tp = q.plan_program(seg, n // 2, na, nb, w["order"], w["steps"])["touches_per_power"] * ((1 << P) - 1)
+        tp = touches_of[(n, na, nb, id(seg))] * total
         total_touch += tp
         total_t += tp / rate[n]
-    return total_touch / total_t, max(cores.values()), "one instance per size, one at a time: " + "; ".join(parts)
+    return total_touch / total_t, max(cores.values()), {
+        "what": "one instance per size, one at a time, fastest of " + str(thread_choices()) + " threads: " +
+                "; ".join(parts), "powers_sampled": sampled, "powers_total": total * len(terms),
+        "touches_per_step": total_touch}
 
 
 def batch_phase_check(q, progs, P, b0, probs64, device):
@@ -543,22 +647,20 @@ def run_batch(args, w, rank, ws, local):
     value = touches * ws / (ms_step / 1e3)
     peak, peak_kind = peaks()
     achieved = touches * 16 / (ms_step / 1e3) / 1e9
-    sizes = {}
-    for n, na, nb, seg in terms:
-        sizes[n] = sizes.get(n, 0) + 1
     line = {
         "metric": "amplitude-term updates/s per Trotter step", "value": value, "unit": "touches/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: seeded integrals (h_pq ~ N(0,1) exp(-|p-q|/2), (pq|rs) ~ N(0,0.1^2) "
-                "exp(-(|p-q|+|r-s|)/3)), one seed per instance, one batch per rank",
-        "config": {"workload": args.workload, "description": w["desc"], "instances": len(terms),
-                   "instances_per_n": {str(k): v for k, v in sorted(sizes.items())}, "precision": P, "dt": w["dt"],
-                   "state": w["dtype"], "touches_per_step": touches, "classes": info["classes"],
-                   "l2": "flushed before every timed step", "parallelism": f"replicas x{ws}"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA_NOTE.replace(
+            "Hartree-Fock start", "one seed per instance, Hartree-Fock starts"),
+        "config": batch_config(args, w, terms, touches, ws),
+        "classes": info["classes"],
+        "roofline": {"bound": "latency", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_kind,
-                     "kernel": "k_pass (batched tile passes), 16 algorithmic bytes per touch over the whole run"},
+                     "peak_note": f"{peak_kind} HBM copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
+                     "kernel": "k_pass (batched tile passes), 16 algorithmic bytes per touch over the whole run",
+                     "bound_note": "every class's complex64 working blocks stay in L2 across the passes; the tile "
+                                   "passes wait on L2 round trips and per-pass launches, so the algorithmic HBM "
+                                   "figure is a ceiling reference, not the binding resource"},
         "e2e": {"value": touches * ws / (e2e_ms / args.steps / 1e3), "unit": "touches/s",
                 "h2d_bytes_per_step": int(sum(a.nbytes for a in b0)),
                 "d2h_bytes_per_step": int(probs.nbytes)},
@@ -580,56 +682,69 @@ def run_batch(args, w, rank, ws, local):
     if w.get("check_c128") and w["dtype"] == "c64":
         line["precision_check"] = batch_phase_check(q, progs, P, b0, probs, local)
     if rank == 0 and not args.no_cpu_baseline:
-        r, cores, sample = cpu_baseline_batch(q, w, terms)
-        line["cpu_baseline"] = {"value": r, "unit": "touches/s", "cores": cores, "kind": "port", "sample": sample}
+        r, cores, sample = cpu_baseline_batch(graft.load_oracle().Oracle(fast=True), w, terms)
+        line["cpu_baseline"] = {"value": r, "unit": "touches/s", "cores": cores, "kind": "port",
+                                "sample": sample["what"], "powers_sampled": sample["powers_sampled"],
+                                "powers_total": sample["powers_total"]}
     return line
 
 
 def run_reference(args, w, rank, ws):
+    """The reference arm: the CPU restatement of the reference's path (oracle/,
+    liborc_fast.so) on the host cores, at its fastest thread count, on the same
+    workload. It loads neither the package nor its library: the integrals come
+    from the workload generator's file, the terms from the oracle's own term
+    compiler and the touch counts from the oracle's run tables. Every step is a
+    bounded sample of the workload (the first controlled powers from the
+    Hartree-Fock start, sized so that the steps end within a few minutes);
+    ms_per_step is the sample's own time."""
     if rank != 0:
         return None
-    q = graft.load_package()
     if w.get("learned"):
         return {"impl": "reference", "unavailable": "the reference has no learned initial state (Hartree-Fock "
                                                     "only); the Hartree-Fock arm is part of this workload's own line"}
+    orc = graft.load_oracle().Oracle(fast=True)
+    per_step_s = max(2.0, 60.0 / max(args.steps, 1))
     if w.get("batch"):
-        terms = build_batch_terms(q, w)
-        rates = []
+        terms = build_batch_terms_oracle(orc, w)
+        r, cores, sample = cpu_baseline_batch(orc, w, terms, budget_s=2.0)  # warm-up and thread choice
+        rates, secs = [], []
         for _ in range(args.steps):
-            r, cores, sample = cpu_baseline_batch(q, w, terms, budget_s=max(10.0, 60.0 / max(args.steps, 1)))
+            r, cores, sample = cpu_baseline_batch(orc, w, terms, budget_s=per_step_s)
             rates.append(r)
+            secs.append(per_step_s)
         value = statistics.median(rates)
-        touches = sum(q.plan_program(seg, n // 2, na, nb, w["order"], w["steps"])["touches_per_power"]
-                      for n, na, nb, seg in terms) * ((1 << w["P"]) - 1)
-        return {"metric": "amplitude-term updates/s per Trotter step", "value": value, "unit": "touches/s",
-                "impl": "reference", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": touches / value * 1e3, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic (same integrals as the GPU arm)",
-                "config": {"workload": args.workload, "description": w["desc"]},
-                "cpu_baseline": {"value": value, "unit": "touches/s", "cores": cores, "kind": "port",
-                                 "sample": sample + "; CPU restatement of the reference (oracle/qpe_oracle.cc), "
-                                                    "complex128: the reference has no complex64 path"},
-                "e2e": {"value": value, "unit": "touches/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    h, seg = build_problem(q, w)
-    rates = []
-    sample = ""
-    threads = 1
-    for _ in range(args.warmup and 1):
-        cpu_baseline(q, w, seg, budget_s=2.0)
-    for _ in range(args.steps):
-        r, threads, sample = cpu_baseline(q, w, seg, budget_s=max(5.0, 60.0 / max(args.steps, 1)))
-        rates.append(r)
-    value = statistics.median(rates)
-    M, e, P = w["n"] // 2, w["N"] // 2, w["P"]
-    touches_step = q.plan_program(seg, M, e, e, w["order"], w["steps"])["touches_per_power"] * ((1 << P) - 1)
+        touches = sample["touches_per_step"]
+        cfg = batch_config(args, w, terms, touches, ws)
+        what = sample["what"]
+        sampled, total = sample["powers_sampled"], sample["powers_total"]
+    else:
+        seg = oracle_terms(orc, w, w["n"], w["N"] // 2, w["seed"])
+        cpu_baseline(orc, w, seg, budget_s=1.0)  # warm-up
+        rates, secs = [], []
+        for _ in range(args.steps):
+            r, cores, sample = cpu_baseline(orc, w, seg, budget_s=per_step_s)
+            rates.append(r)
+            secs.append(sample["seconds"])
+        value = statistics.median(rates)
+        cfg = workload_config(args, w, sample["touches_per_power"], ws)
+        touches = cfg["touches_per_step"]
+        what = sample["what"]
+        sampled, total = sample["powers_sampled"], sample["powers_total"]
+    ms_step = statistics.median(secs) * 1e3
     return {"metric": "amplitude-term updates/s per Trotter step", "value": value, "unit": "touches/s",
             "impl": "reference", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": touches_step / value * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (same integrals as the GPU arm)",
-            "config": {"workload": args.workload, "description": w["desc"]},
-            "cpu_baseline": {"value": value, "unit": "touches/s", "cores": threads, "kind": "port",
-                             "sample": sample + "; CPU restatement of the reference (oracle/qpe_oracle.cc): "
-                                                "the reference's sources are not on this host"},
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (the same integrals as the GPU arm, from the same generator)",
+            "config": cfg,
+            "sample_per_step": {"powers_sampled": sampled, "powers_total": total,
+                                "extrapolated_ms_per_full_step": touches / value * 1e3,
+                                "note": "each step evolves a bounded sample of the workload's controlled powers; "
+                                        "value is the sample's throughput, ms_per_step the sample's time"},
+            "cpu_baseline": {"value": value, "unit": "touches/s", "cores": cores, "kind": "port",
+                             "sample": what + "; CPU restatement of the reference (oracle/qpe_oracle.cc, "
+                                              "oracle/terms_oracle.cc), complex128 (the reference has no complex64 "
+                                              "path); the reference's own build needs its sources, which a GPU host does not have"},
             "e2e": {"value": value, "unit": "touches/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

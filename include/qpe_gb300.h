@@ -78,6 +78,13 @@ int qpe_synchronize(qpe_context* ctx);
 int qpe_timer_record(qpe_context* ctx, uint32_t slot);
 int qpe_timer_elapsed_ms(qpe_context* ctx, uint32_t start_slot, uint32_t end_slot, float* ms);
 
+/* Measures the device's FP64 FMA throughput (TFLOP/s, an FMA counting 2): a
+ * kernel of 8 independent FMA chains per thread on 4 x 256-thread CTAs per SM,
+ * timed with CUDA events on the context's stream (slots 14 and 15). A
+ * measurement helper for reporting FP64 roofline fractions; no counterpart in
+ * the reference. */
+int qpe_measure_fp64_peak(qpe_context* ctx, double* tflops);
+
 /* Page-locked host memory (cudaMallocHost), for host buffers the copies of
  * the one-shot and resident APIs read and write at full speed. */
 int qpe_host_alloc(size_t bytes, void** out);
@@ -86,6 +93,16 @@ int qpe_host_free(void* p);
 /* Writes a 256 MiB device buffer (allocated on first use) so that the next
  * timed region starts with nothing of the state in L2. */
 int qpe_flush_l2(qpe_context* ctx);
+
+/* Self-test of the bounded device waits (no counterpart in the reference, which
+ * only asserts: cpp/offset_computer.hpp:39,47). Every wait of the library's
+ * tcgen05 / TMA kernels polls an mbarrier a bounded number of times, and a wait
+ * that runs out makes the kernel record an error and return, so the call reports
+ * QPE_ERR_TIMEOUT and the context stays usable. This runs that wait alone on one
+ * mbarrier with nothing else in flight: with arrive = 0 nobody completes it, the
+ * wait gives up after max_tries polls and the call returns QPE_ERR_TIMEOUT; with
+ * arrive = 1 a thread completes it first and the call returns QPE_OK. */
+int qpe_selftest_bounded_wait(qpe_context* ctx, uint32_t max_tries, int arrive);
 
 /* ---- combinatorial primitives (device kernels) ------------------------------ */
 
@@ -282,20 +299,23 @@ typedef struct qpe_batch_class {
 int qpe_batch_class_info(const qpe_batch* b, uint32_t cls, qpe_batch_class* out);
 
 /* ---- QIFT without any allocation ------------------------------------------------
- * No counterpart in the reference. For callers that cannot allocate device memory
- * when they need the QIFT: code whose stream is being captured into a CUDA graph
- * (cudaMalloc is not allowed during capture), or a host that hands out all device
- * memory from its own pool. Runs the QIFT of qpe_state_qift in place on the
- * caller's device register d_state (2^precision x ld elements of dtype) on the
- * caller's cudaStream_t `stream` and writes the phase histogram (2^precision
- * doubles) to the device buffer d_probs. It calls no allocator: the kernel's
- * scratch (histogram partial rows and twiddles) is one fixed array of
- * QPE_NOALLOC_SCRATCH_DOUBLES doubles (about 2 MiB) inside the library, which
- * every GPU that loads the library holds until the process exits; precision
+ * No counterpart in the reference. For callers that cannot let a library allocate
+ * device memory: a host application that hands out all device memory from its own
+ * pool and forbids libraries from taking more, or a latency-bound loop that cannot
+ * afford cudaMalloc / cudaFree (which may synchronise the device). Runs the QIFT of
+ * qpe_state_qift in place on the caller's device register d_state (2^precision x
+ * ld elements of dtype) on the caller's cudaStream_t `stream` and writes the phase
+ * histogram (2^precision doubles) to the device buffer d_probs. It calls no
+ * allocator: the kernel's scratch (histogram partial rows, about 2 MiB) and the
+ * twiddle tables of every precision (24 KiB) are fixed arrays inside the library,
+ * which every GPU that loads the library holds until the process exits; precision
  * above QPE_NOALLOC_MAX_PRECISION is rejected with QPE_ERR_UNSUPPORTED. The first
- * call on a device sets up the array's device address (cudaGetSymbolAddress), so
- * make it before any stream capture. All calls share the array: calls that
- * overlap on the GPU (other streams, other host threads) race on it. */
+ * call on a device, with that device current, does the set-up: it looks up the
+ * arrays' device addresses (cudaGetSymbolAddress), fills the twiddle tables with a
+ * synchronous copy and sets the QIFT kernel's shared-memory limit; make that first
+ * call before any stream capture. Later calls only launch kernels on `stream`.
+ * All calls share the partial rows: calls that overlap on the GPU (other streams,
+ * other host threads) race on them. */
 #define QPE_NOALLOC_MAX_PRECISION 10
 #define QPE_NOALLOC_MAX_CTAS 256
 #define QPE_NOALLOC_SCRATCH_DOUBLES ((QPE_NOALLOC_MAX_CTAS << QPE_NOALLOC_MAX_PRECISION) + (1 << QPE_NOALLOC_MAX_PRECISION))

@@ -20,7 +20,21 @@ ORC_LIB = HERE / "build" / "liborc.so"
 ORC_FAST_LIB = HERE / "build" / "liborc_fast.so"
 REF_LIB = HERE / "_ref" / "libref.so"
 REF_FAST_LIB = HERE / "_ref" / "libref_fast.so"
-REF_SRC = Path(os.environ.get("QPE_REFERENCE_CPP", "/root/reference/cpp"))
+
+
+def reference_cpp() -> Path | None:
+    """The reference's cpp/ directory where its sources are present: the
+    QPE_REFERENCE_CPP environment variable, else the default of the oracle's
+    build recipe (Makefile); None where neither exists (as on a GPU host)."""
+    env = os.environ.get("QPE_REFERENCE_CPP")
+    if env:
+        return Path(env) if Path(env).is_dir() else None
+    try:
+        out = subprocess.run(["make", "-s", "-C", str(HERE), "print-ref"], capture_output=True, text=True,
+                             check=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return None
+    return Path(out) if out and Path(out).is_dir() else None
 
 
 class QpeTerm(C.Structure):
@@ -47,13 +61,15 @@ def _elf_matches(path: Path) -> bool:
 
 def build(ref: bool | None = None) -> None:
     """Builds the oracle (and, when the reference sources exist, oracle/_ref)."""
+    src = reference_cpp()
     targets = ["all"]
-    if ref or (ref is None and REF_SRC.is_dir()):
+    if ref or (ref is None and src is not None):
         targets.append("ref")
     for t in (ORC_LIB, ORC_FAST_LIB, REF_LIB, REF_FAST_LIB):
         if t.exists() and not _elf_matches(t):
             t.unlink()
-    subprocess.run(["make", "-s", "-C", str(HERE), f"REF={REF_SRC}", *targets], check=True)
+    extra = [f"REF={src}"] if src is not None else []
+    subprocess.run(["make", "-s", "-C", str(HERE), *extra, *targets], check=True)
 
 
 def _ptr(a: np.ndarray, ct=C.c_double):
@@ -105,6 +121,17 @@ class Oracle:
                                           C.c_size_t]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_touches_per_power.restype = C.c_uint64
+        L.orc_touches_per_power.argtypes = [C.c_uint, C.c_uint, C.c_uint, P, C.c_size_t, P, C.c_size_t, P,
+                                            C.c_size_t, P, C.c_size_t, P, C.c_size_t, C.c_uint, C.c_uint]
+        L.orc_terms_create.restype = C.c_void_p
+        L.orc_terms_destroy.argtypes = [C.c_void_p]
+        L.orc_terms_set.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.c_double]
+        L.orc_terms_add_one_body.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
+        L.orc_terms_add_two_body.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]
+        L.orc_terms_segments.restype = C.c_int
+        L.orc_terms_segments.argtypes = [C.c_void_p, C.POINTER(C.c_size_t), C.POINTER(P),
+                                         C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_size_t)]
 
     def nchoosek(self, n, k):
         return int(self.lib.orc_nchoosek(n, k))
@@ -173,6 +200,45 @@ class Oracle:
         if rc:
             raise RuntimeError("orc_rank_with_swaps failed")
         return out
+
+    def segmented_terms(self, num_orbitals, num_occupied, t, one_body, two_body, with_raw=False):
+        """The oracle's term compiler (terms_oracle.cc): AddOneBodyTerm(p, q, v) for
+        each (p, q, v) of one_body, AddTwoBodyTerm(p, q, r, s, v) for each
+        (p, q, r, s, v) of two_body, IndexTerms, then the five segments with the
+        getters' coefficients at timestep t. Returns kind -> TERM_DTYPE array (and
+        kind -> indexed values with with_raw)."""
+        L = self.lib
+        h = L.orc_terms_create()
+        try:
+            L.orc_terms_set(h, num_orbitals, num_occupied, t)
+            for p, q, v in one_body:
+                L.orc_terms_add_one_body(h, int(p), int(q), float(v))
+            for p, q, r, s_, v in two_body:
+                L.orc_terms_add_two_body(h, int(p), int(q), int(r), int(s_), float(v))
+            counts = (C.c_size_t * 5)()
+            if L.orc_terms_segments(h, counts, None, None, None):
+                raise RuntimeError("orc_terms_segments: unknown term shape")
+            arrs = [np.zeros(int(counts[k]), TERM_DTYPE) for k in range(5)]
+            raws = [np.zeros(int(counts[k])) for k in range(5)]
+            P = C.POINTER(QpeTerm)
+            outs = (P * 5)(*[a.ctypes.data_as(P) for a in arrs])
+            rptr = (C.POINTER(C.c_double) * 5)(*[_ptr(r) for r in raws])
+            caps = (C.c_size_t * 5)(*[len(a) for a in arrs])
+            if L.orc_terms_segments(h, counts, outs, rptr, caps):
+                raise RuntimeError("orc_terms_segments failed")
+        finally:
+            L.orc_terms_destroy(h)
+        kinds = ("pp", "pq", "pqqp", "pqqr", "pqrs")
+        seg = dict(zip(kinds, arrs))
+        return (seg, dict(zip(kinds, raws))) if with_raw else seg
+
+    def touches_per_power(self, M, na, nb, seg, order=1, steps=1):
+        """Amplitude updates of one controlled power, counted from the oracle's run
+        tables (2 per pair update, 1 per diagonal phase)."""
+        args = []
+        for k in ("pp", "pq", "pqqp", "pqqr", "pqrs"):
+            args += list(terms_ptr(seg.get(k)))
+        return int(self.lib.orc_touches_per_power(M, na, nb, *args, order, steps))
 
     def set_threads(self, n):
         self.lib.orc_set_threads(int(n))

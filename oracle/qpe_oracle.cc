@@ -199,6 +199,17 @@ struct Geom {
   uint64_t Ca, Cb, block;
 };
 
+// Touch counting (orc_touches_per_power): while set, every update primitive adds
+// the amplitude updates it would make (2 per pair, 1 per diagonal phase) and
+// returns without touching the block.
+static uint64_t* g_touches = nullptr;
+
+static uint64_t run_total(const std::vector<Run>& r) {
+  uint64_t n = 0;
+  for (const Run& x : r) n += x.niter;
+  return n;
+}
+
 static inline void coeffs_of(const qpe_term& t, unsigned par, cplx& c0, cplx& c1) {
   const double* m = (par & 1) ? t.odd : t.even;
   c0 = cplx(m[0], m[1]);
@@ -216,6 +227,10 @@ static inline void pair_update(cplx* sv, const cplx& c0, const cplx& c1, uint64_
 // Row-pair x all-columns update (_updateAAAA :591-659 and updatePQ_AA :927-958).
 static void rows_pairs_all_cols(cplx* blk, const Geom& g, const std::vector<Run>& ra,
                                 const qpe_term& t) {
+  if (g_touches) {
+    *g_touches += 2 * run_total(ra) * g.Cb;
+    return;
+  }
   std::vector<uint64_t> goal(ra.size() + 1, 0);
   for (size_t i = 0; i < ra.size(); ++i) goal[i + 1] = goal[i] + ra[i].niter;
   const int64_t total = (int64_t)goal.back();
@@ -234,6 +249,10 @@ static void rows_pairs_all_cols(cplx* blk, const Geom& g, const std::vector<Run>
 // All-rows x column-pair update (_updateBBBB :661-735 and updatePQ_BB :959-986).
 static void all_rows_cols_pairs(cplx* blk, const Geom& g, const std::vector<Run>& rb,
                                 const qpe_term& t) {
+  if (g_touches) {
+    *g_touches += 2 * g.Ca * run_total(rb);
+    return;
+  }
 #pragma omp parallel for schedule(static)
   for (int64_t a = 0; a < (int64_t)g.Ca; ++a) {
     const uint64_t row = (uint64_t)a * g.Cb;
@@ -250,6 +269,10 @@ static void all_rows_cols_pairs(cplx* blk, const Geom& g, const std::vector<Run>
 // parity is the sum of both sides' run parities (:774).
 static void rows_pairs_cols_runs(cplx* blk, const Geom& g, const std::vector<Run>& ra,
                                  const std::vector<Run>& rb, const qpe_term& t) {
+  if (g_touches) {
+    *g_touches += 2 * run_total(ra) * run_total(rb);
+    return;
+  }
   std::vector<uint64_t> goal(ra.size() + 1, 0);
   for (size_t i = 0; i < ra.size(); ++i) goal[i + 1] = goal[i] + ra[i].niter;
   const int64_t total = (int64_t)goal.back();
@@ -270,6 +293,10 @@ static void rows_pairs_cols_runs(cplx* blk, const Geom& g, const std::vector<Run
 // Row-list x column-pair update (updatePQQR_BAAB :1109-1158).
 static void rows_list_cols_pairs(cplx* blk, const Geom& g, const std::vector<Run>& ra,
                                  const std::vector<Run>& rb, const qpe_term& t) {
+  if (g_touches) {
+    *g_touches += 2 * run_total(ra) * run_total(rb);
+    return;
+  }
 #pragma omp parallel for
   for (int64_t ia = 0; ia < (int64_t)ra.size(); ++ia) {
     for (uint64_t na = 0; na < ra[ia].niter; ++na) {
@@ -285,6 +312,10 @@ static void rows_list_cols_pairs(cplx* blk, const Geom& g, const std::vector<Run
 
 // Diagonal phase on row-list x all columns (updatePP_AA :886-906, updatePQQP_AA :988-1014).
 static void diag_rows(cplx* blk, const Geom& g, const std::vector<Run>& ra, const cplx& c) {
+  if (g_touches) {
+    *g_touches += run_total(ra) * g.Cb;
+    return;
+  }
 #pragma omp parallel for
   for (int64_t ia = 0; ia < (int64_t)ra.size(); ++ia)
     for (uint64_t na = 0; na < ra[ia].niter; ++na) {
@@ -295,6 +326,10 @@ static void diag_rows(cplx* blk, const Geom& g, const std::vector<Run>& ra, cons
 
 // Diagonal phase on all rows x column-list (updatePP_BB :907-925, updatePQQP_BB :1015-1039).
 static void diag_cols(cplx* blk, const Geom& g, const std::vector<Run>& rb, const cplx& c) {
+  if (g_touches) {
+    *g_touches += g.Ca * run_total(rb);
+    return;
+  }
 #pragma omp parallel for
   for (int64_t a = 0; a < (int64_t)g.Ca; ++a) {
     const uint64_t row = (uint64_t)a * g.Cb;
@@ -306,6 +341,10 @@ static void diag_cols(cplx* blk, const Geom& g, const std::vector<Run>& rb, cons
 // Diagonal phase on row-list x column-list (updatePQQP_AB :1040-1071).
 static void diag_rows_cols(cplx* blk, const Geom& g, const std::vector<Run>& ra,
                            const std::vector<Run>& rb, const cplx& c) {
+  if (g_touches) {
+    *g_touches += run_total(ra) * run_total(rb);
+    return;
+  }
 #pragma omp parallel for
   for (int64_t ia = 0; ia < (int64_t)ra.size(); ++ia)
     for (uint64_t na = 0; na < ra[ia].niter; ++na) {
@@ -473,6 +512,24 @@ int orc_time_evolve(unsigned M, unsigned ea, unsigned eb, unsigned P, const qpe_
     }
   }
   return QPE_OK;
+}
+
+// Amplitude updates of one controlled power (order 2: a forward and a reversed
+// sweep per step; `steps` steps): each primitive counts 2 per pair update and 1
+// per diagonal phase, from the same run tables it would apply.
+uint64_t orc_touches_per_power(unsigned M, unsigned ea, unsigned eb, const qpe_term* pp, size_t npp,
+                               const qpe_term* pq, size_t npq, const qpe_term* pqqp, size_t npqqp,
+                               const qpe_term* pqqr, size_t npqqr, const qpe_term* pqrs, size_t npqrs,
+                               unsigned order, unsigned steps) {
+  if (M == 0 || M > 31 || ea > M || eb > M) return 0;
+  Geom g{M, ea, eb, nck((int)M, (int)ea), nck((int)M, (int)eb), 0};
+  g.block = g.Ca * g.Cb;
+  Terms T{pp, pq, pqqp, pqqr, pqrs, npp, npq, npqqp, npqqr, npqrs};
+  uint64_t n = 0;
+  g_touches = &n;
+  sweep(nullptr, g, T, false);
+  g_touches = nullptr;
+  return n * (order == 2 ? 2 : 1) * (steps ? steps : 1);
 }
 
 // time_evolve_iqpe (:141-155): block 1 of the register, in place, receives

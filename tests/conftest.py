@@ -42,6 +42,13 @@ def gpu(q):
     return q
 
 
+def reference_root():
+    """The reference tree (its cpp/ directory's parent) where its sources are
+    present, else None; located as the oracle's build recipe locates it."""
+    src = graft.load_oracle().reference_cpp()
+    return src.parent if src is not None else None
+
+
 def load_golden(name):
     return np.load(GOLDEN / name)
 

@@ -59,11 +59,18 @@ def seg_arrays(seg, raw, prefix=""):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-dir", default=os.environ.get("QPE_REFERENCE_DIR", "/root/reference"))
+    ap.add_argument("--reference-dir", default=os.environ.get("QPE_REFERENCE_DIR"),
+                    help="the reference tree (default: where the oracle's build recipe finds it)")
     a = ap.parse_args()
-    refdir = Path(a.reference_dir)
-    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), f"REF={refdir / 'cpp'}", "ref"], check=True)
     import __graft_entry__ as g
+    if a.reference_dir:
+        refdir = Path(a.reference_dir)
+    else:
+        src = g.load_oracle().reference_cpp()
+        if src is None:
+            raise SystemExit("the reference sources are not present: pass --reference-dir")
+        refdir = src.parent
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), f"REF={refdir / 'cpp'}", "ref"], check=True)
     q = g.load_package()
     O = g.load_oracle()
     ref = O.Reference()

@@ -91,6 +91,54 @@ def test_sector_hamiltonian_and_trotter_order(q, orc, n, seed):
     assert 3.0 < errs[0] / errs[1] < 5.0, errs
 
 
+def _power(q, orc, M, e, ints, psi, dt, order, steps):
+    """One controlled power of total time dt in `steps` Trotter steps: order 1
+    sweeps at dt / steps, order 2 a forward and a reversed sweep at dt / (2 steps)
+    each (the coefficient time the plain-n16 workload uses is dt / 2 per sweep)."""
+    t = dt / (2 * steps) if order == 2 else dt / steps
+    seg = q.Hamiltonian.from_integrals(ints, e, t).segmented_terms()
+    d = len(psi)
+    st = np.zeros(2 * d, complex)
+    st[:d] = psi
+    orc.time_evolve(M, e, e, 1, seg, st, order=order, steps=steps)
+    return st[d:]
+
+
+@pytest.mark.parametrize("n,seed", [(8, 0), (8, 5), (10, 2)])
+def test_second_order_trotter_is_second_order(q, orc, n, seed):
+    """The order-2 extension (a forward and a reversed sweep per step, the mode
+    the plain-n16 workload runs with 4 steps per power; the reference has first
+    order only, cpp/time_evolution_over_terms.hpp:116-137) against exp(-i H dt)
+    of the sector Hamiltonian read back from the sweep:
+    - its one-step error falls about 8x from dt to dt / 2 (local error dt^3),
+      where first order falls about 4x (dt^2);
+    - four order-2 steps of dt / 4 are about 16x closer than one step of dt;
+    - as dt -> 0, four order-2 steps converge to one first-order step, their
+      difference falling about 4x per halving (it is first order's dt^2 error)."""
+    M, e = n // 2, n // 4
+    ints = q.synthetic_integrals(n, seed)
+    H, _ = _sector_hamiltonian(q, orc, M, e, ints)
+    d = H.shape[0]
+    rng = np.random.default_rng(100 + seed)
+    psi = rng.standard_normal(d) + 1j * rng.standard_normal(d)
+    psi /= np.linalg.norm(psi)
+    dts = (0.04, 0.02, 0.01)
+    exact = {dt: expm(-1j * H * dt) @ psi for dt in dts}
+    e1 = [np.linalg.norm(_power(q, orc, M, e, ints, psi, dt, 1, 1) - exact[dt]) for dt in dts]
+    e2 = [np.linalg.norm(_power(q, orc, M, e, ints, psi, dt, 2, 1) - exact[dt]) for dt in dts]
+    e24 = [np.linalg.norm(_power(q, orc, M, e, ints, psi, dt, 2, 4) - exact[dt]) for dt in dts]
+    diff = [np.linalg.norm(_power(q, orc, M, e, ints, psi, dt, 2, 4) - _power(q, orc, M, e, ints, psi, dt, 1, 1))
+            for dt in dts]
+    for i in range(2):
+        assert 3.0 < e1[i] / e1[i + 1] < 5.0, e1
+        assert 6.0 < e2[i] / e2[i + 1] < 10.0, e2
+        assert 6.0 < e24[i] / e24[i + 1] < 10.0, e24
+        assert 3.0 < diff[i] / diff[i + 1] < 5.0, diff
+    for i in range(3):
+        assert 10.0 < e2[i] / e24[i] < 22.0, (e2, e24)
+        assert e2[i] < e1[i]
+
+
 def test_qpe_energy_on_the_spectrum(q, orc):
     n, seed, P, dt = 8, 3, 10, 0.05
     M, e = n // 2, n // 4

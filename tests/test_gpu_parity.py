@@ -245,6 +245,39 @@ def test_strategies_bit_identical(gpu, orc, strategy, cluster, n, na, nb, P):
     assert np.array_equal(st.download(), ref)
 
 
+@pytest.mark.parametrize("strategy,cluster", [(0, 0), (6, 16), (6, 8), (3, 0)])
+def test_headline_configuration(gpu, orc, strategy, cluster):
+    """The plain-n16 bench workload exactly as it is timed, at P = 3: n = 16,
+    N = 8, seed-0 integrals, 2nd-order Trotter (forward and reversed sweeps at
+    dt / 2 = 0.025), 4 steps per power, Hartree-Fock start, complex128. Autotuned
+    (the strategy the bench ends up with) and forced to the three-warp-group
+    cluster of 16 and 8 CTAs and to the tile passes: the register is bit-identical
+    to the oracle's order-2, 4-step evolution, and after the QIFT the register too,
+    and the histogram within 1e-12."""
+    q = gpu
+    n, N, P, dt, order, steps = 16, 8, 3, 0.05, 2, 4
+    M, e = n // 2, N // 2
+    h = q.Hamiltonian.from_integrals(q.synthetic_integrals(n, 0), e, dt / 2)
+    seg = h.segmented_terms()
+    prog = q.Program(seg, M, e, e, trotter_order=order, steps=steps)
+    assert prog.touches_per_power == 24_304_000
+    st = q.DeviceState(M, e, e, P)
+    b0 = q.hf_block0(st.c_alpha, st.c_beta, P)
+    st.upload(b0)
+    st.evolve(prog, strategy=strategy, cluster_size=cluster)
+    if strategy == 6:
+        assert st.last_strategy() == (6, cluster)
+    ref = np.zeros(st.size, np.complex128)
+    ref[:st.ld] = b0
+    orc.time_evolve(M, e, e, P, seg, ref, order=order, steps=steps)
+    assert np.array_equal(st.download(), ref)
+    st.qift()
+    orc.qift(P, st.ld, ref)
+    assert np.array_equal(st.download(), ref)
+    np.testing.assert_allclose(st.phase_probs(), orc.identify_phase_amplitudes(P, st.ld, ref), rtol=1e-12,
+                               atol=1e-16)
+
+
 @pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0), (4, 1), (4, 4), (5, 1), (5, 4), (6, 1), (6, 4)])
 def test_strategies_complex64(gpu, orc, strategy, cluster):
     q = gpu

@@ -108,3 +108,33 @@ def test_oracle_pp_fixture_phase(orc):
     orc.qift(P, 1, s)
     probs = orc.identify_phase_amplitudes(P, 1, s)
     assert probs[87] > 0.5
+
+
+@pytest.mark.parametrize("name", sorted(p.name for p in GOLDEN.glob("terms_*.npz")))
+def test_oracle_term_compiler_matches_reference(q, orc, name):
+    """The oracle's own term compiler (oracle/terms_oracle.cc) gives the
+    reference's segmented terms, indexed values and getter coefficients."""
+    from test_term_compiler import KINDS, _assert_segments
+    z = load_golden(name)
+    n, N, dt, seed = int(z["n"]), int(z["N"]), float(z["dt"]), int(z["seed"])
+    ints = q.synthetic_integrals(n, seed)
+    seg, raw = orc.segmented_terms(n // 2, N // 2, dt, ints.one_body, ints.two_body, with_raw=True)
+    _assert_segments(seg, golden_segments(z))
+    for k in KINDS:
+        np.testing.assert_array_equal(raw[k], z[k + "_raw"])
+
+
+@pytest.mark.parametrize("n,na,nb,order,steps", [(8, 2, 2, 1, 1), (16, 4, 4, 1, 1), (16, 4, 4, 2, 4),
+                                                  (12, 3, 2, 1, 1), (10, 1, 1, 2, 3), (20, 5, 5, 1, 1)])
+def test_oracle_touch_counts(q, orc, n, na, nb, order, steps):
+    """Amplitude updates per controlled power counted from the oracle's run
+    tables: the survey's counts of the reference (n = 8: 2,160, n = 16: 3,038,000
+    per first-order step) and the product's program planner's counts."""
+    ints = q.synthetic_integrals(n, 1)
+    seg = orc.segmented_terms(n // 2, max(na, nb), 0.05, ints.one_body, ints.two_body)
+    got = orc.touches_per_power(n // 2, na, nb, seg, order, steps)
+    assert got == q.plan_program(seg, n // 2, na, nb, order, steps)["touches_per_power"]
+    known = {(8, 2, 2, 1, 1): 2160, (16, 4, 4, 1, 1): 3_038_000, (16, 4, 4, 2, 4): 24_304_000,
+             (20, 5, 5, 1, 1): 87_635_520}
+    if (n, na, nb, order, steps) in known:
+        assert got == known[(n, na, nb, order, steps)]
