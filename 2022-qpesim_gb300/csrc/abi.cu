@@ -145,9 +145,23 @@ static void build_device_program(qpe_program* pr) {
 }
 
 // Launch geometry of one pass for elements of esz bytes.
+void check_device_error(qpe_context* ctx) {
+  int e = 0;
+  QPE_CK(cudaMemcpyAsync(&e, ctx->err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QPE_CK(cudaStreamSynchronize(ctx->stream));
+  if (e) {
+    QPE_CK(cudaMemsetAsync(ctx->err.p, 0, sizeof(int), ctx->stream));
+    QPE_CK(cudaStreamSynchronize(ctx->stream));
+    throw Error(QPE_ERR_TIMEOUT, "a tile pass's bounded wait for its bulk copies ran out (code " + std::to_string(e) +
+                                     "); the affected results are invalid");
+  }
+}
+
 PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_optin, const Pass& pass) {
   const HostProgram& hp = pr->hp;
   PassLaunch pl{};
+  pl.err = pr->ctx->err.as<int>();
+  pl.bulk = (pass.type != PASS_ROW && (hp.Ca * esz) % 16 == 0) ? 1u : 0u;
   pl.pool = pr->pool.as<uint32_t>();
   pl.ops = pr->ops.as<DevOp>();
   pl.coef = pr->coef.as<double>();
@@ -626,6 +640,8 @@ int qpe_context_create(int device, qpe_context** out) {
       host_ref_binom_table(tb.data());
       ctx->binom.alloc(tb.size() * sizeof(uint64_t));
       QPE_CK(cudaMemcpy(ctx->binom.p, tb.data(), tb.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+      ctx->err.alloc(16);
+      QPE_CK(cudaMemset(ctx->err.p, 0, 16));
     } catch (...) {
       if (ctx->stream) cudaStreamDestroy(ctx->stream);
       delete ctx;
@@ -652,6 +668,7 @@ int qpe_synchronize(qpe_context* ctx) {
   return guard([&] {
     check_ctx(ctx);
     QPE_CK(cudaStreamSynchronize(ctx->stream));
+    check_device_error(ctx);
   });
 }
 
@@ -689,14 +706,24 @@ int qpe_measure_fp64_peak(qpe_context* ctx, double* tflops) {
     DevBuf out;
     const uint32_t ctas = (uint32_t)ctx->num_sms * 4, threads = 256, iters = 4096;
     out.alloc((size_t)ctas * threads * sizeof(double));
+    cudaEvent_t ev[2] = {};
+    QPE_CK(cudaEventCreate(&ev[0]));
+    struct Events {
+      cudaEvent_t* e;
+      ~Events() {
+        for (int i = 0; i < 2; ++i)
+          if (e[i]) cudaEventDestroy(e[i]);
+      }
+    } guard_events{ev};
+    QPE_CK(cudaEventCreate(&ev[1]));
     QPE_CK(launch_fp64_fma_probe(out.as<double>(), ctas, threads, iters, ctx->stream));  // warm-up
-    QPE_CK(cudaEventRecord(ctx->events[14], ctx->stream));
+    QPE_CK(cudaEventRecord(ev[0], ctx->stream));
     const int reps = 4;
     for (int r = 0; r < reps; ++r) QPE_CK(launch_fp64_fma_probe(out.as<double>(), ctas, threads, iters, ctx->stream));
-    QPE_CK(cudaEventRecord(ctx->events[15], ctx->stream));
-    QPE_CK(cudaEventSynchronize(ctx->events[15]));
+    QPE_CK(cudaEventRecord(ev[1], ctx->stream));
+    QPE_CK(cudaEventSynchronize(ev[1]));
     float ms = 0.f;
-    QPE_CK(cudaEventElapsedTime(&ms, ctx->events[14], ctx->events[15]));
+    QPE_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
     const double flops = 2.0 * kFp64ProbeChains * (double)iters * ctas * threads * reps;
     *tflops = flops / (ms * 1e-3) / 1e12;
   });
@@ -953,6 +980,7 @@ int qpe_state_download(qpe_state* st, void* host, uint64_t first, uint64_t count
     QPE_CK(cudaMemcpyAsync(host, st->data.as<char>() + first * st->esz, count * st->esz, cudaMemcpyDeviceToHost,
                            st->ctx->stream));
     QPE_CK(cudaStreamSynchronize(st->ctx->stream));
+    check_device_error(st->ctx);
   });
 }
 
@@ -994,6 +1022,7 @@ int qpe_state_phase_probs(qpe_state* st, double* probs) {
     }
     QPE_CK(cudaMemcpyAsync(probs, st->probs.p, st->N * sizeof(double), cudaMemcpyDeviceToHost, st->ctx->stream));
     QPE_CK(cudaStreamSynchronize(st->ctx->stream));
+    check_device_error(st->ctx);
   });
 }
 

@@ -61,6 +61,7 @@ struct qpe_context {
   cudaStream_t stream = nullptr;
   qpe::DevBuf binom;
   qpe::DevBuf flush;
+  qpe::DevBuf err;  // device error word of the context's kernels (bounded waits)
   cudaEvent_t events[16] = {};
 };
 
@@ -77,6 +78,9 @@ PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_opt
 std::vector<double> twiddle_table(uint32_t P);
 void state_twiddles(uint32_t P, int dtype, DevBuf& tw);
 void qift_geometry(uint32_t P, uint64_t ld, int dtype, int num_sms, size_t smem_optin, uint32_t& T, uint32_t& grid);
+// Reads and clears the context's device error word (after the stream is
+// synchronised); throws QPE_ERR_TIMEOUT if a kernel's bounded wait ran out.
+void check_device_error(qpe_context* ctx);
 }  // namespace qpe
 
 #endif  // QPE_ABI_INTERNAL_H_

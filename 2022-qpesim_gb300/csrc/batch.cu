@@ -275,7 +275,7 @@ int qpe_batch_create(qpe_context* ctx, uint32_t n, const qpe_program* const* pro
         b->ld.push_back(pr->hp.Ca * pr->hp.Cb);
         b->off.push_back(total);
         total += b->N * b->ld.back();
-        work_total += b->ld.back();
+        work_total += (b->ld.back() + 1) / 2 * 2;  // padded to 16 bytes (see work_off)
         b->touches_per_run += pr->hp.touches_per_power * (b->N - 1);
       }
       b->regs.alloc(total * b->esz);
@@ -297,10 +297,12 @@ int qpe_batch_create(qpe_context* ctx, uint32_t n, const qpe_program* const* pro
       });
       std::vector<uint64_t> work_off(n);
       {
+        // every working block starts on a 16-byte boundary (bulk copies of its columns)
+        const uint64_t align = 16 / b->esz;
         uint64_t o = 0;
         for (uint32_t i = 0; i < n; ++i) {
           work_off[i] = o;
-          o += b->ld[i];
+          o += (b->ld[i] + align - 1) / align * align;
         }
       }
       for (uint32_t i : order) {
@@ -381,6 +383,7 @@ int qpe_batch_download(qpe_batch* b, uint32_t i, void* host, uint64_t first, uin
     QPE_CK(cudaMemcpyAsync(host, b->regs.as<char>() + (b->off[i] + first) * b->esz, count * b->esz,
                            cudaMemcpyDeviceToHost, b->ctx->stream));
     QPE_CK(cudaStreamSynchronize(b->ctx->stream));
+    check_device_error(b->ctx);
   });
 }
 
@@ -402,7 +405,10 @@ int qpe_batch_run(qpe_batch* b, int synchronize) {
     QPE_CK(cudaSetDevice(b->ctx->device));
     if (!b->exec) build_graph(b);
     QPE_CK(cudaGraphLaunch(b->exec, b->ctx->stream));
-    if (synchronize) QPE_CK(cudaStreamSynchronize(b->ctx->stream));
+    if (synchronize) {
+      QPE_CK(cudaStreamSynchronize(b->ctx->stream));
+      check_device_error(b->ctx);
+    }
   });
 }
 
@@ -414,6 +420,7 @@ int qpe_batch_phase_probs(qpe_batch* b, uint32_t i, double* probs) {
     QPE_CK(cudaMemcpyAsync(probs, b->probs.as<double>() + i * b->N, b->N * sizeof(double), cudaMemcpyDeviceToHost,
                            b->ctx->stream));
     QPE_CK(cudaStreamSynchronize(b->ctx->stream));
+    check_device_error(b->ctx);
   });
 }
 

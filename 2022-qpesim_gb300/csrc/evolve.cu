@@ -36,10 +36,56 @@ __device__ __forceinline__ void async_copy(C2* dst, const C2* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
 }
 
-// One pass. PT selects the tile geometry (stage layout [entry][line]):
-//   PASS_COL: tile = W consecutive columns, stage[e * W + w] = block[e][b0 + w]
-//   PASS_ROW: tile = one row,               stage[e]         = block[a][e]
-//   PASS_MIX: tile = columns (b01, b10),    stage[e * 2 + w] = block[e][w ? b10 : b01]
+// Bulk copies between global and shared memory (cp.async.bulk). A load
+// completes on an mbarrier of this CTA (transaction bytes); a store is tracked
+// by the issuing thread's bulk async-group. Addresses and sizes are multiples of
+// 16 bytes.
+__device__ __forceinline__ void bulk_load(void* sdst, const void* gsrc, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   static_cast<uint32_t>(__cvta_generic_to_shared(sdst))),
+               "l"(gsrc), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_store(void* gdst, const void* ssrc, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
+               "r"(static_cast<uint32_t>(__cvta_generic_to_shared(ssrc))), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_init1(uint32_t bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// Bounded wait for the phase of the given parity (about 2^24 polls, far longer
+// than any copy of a tile takes).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  for (uint32_t i = 0; i < (1u << 24); ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// One pass. PT selects the tile geometry; the stage holds a tile by lines:
+//   PASS_COL: tile = W consecutive columns, stage[w * Ca + e] = block[e][b0 + w]
+//   PASS_ROW: tile = one row,               stage[e]          = block[a][e]
+//   PASS_MIX: tile = columns (b01, b10),    stage[w * Ca + e] = block[e][w ? b10 : b01]
+// The working block is stored by columns, so a COL or MIX tile's lines are
+// contiguous runs of it. With pl.bulk they move as whole runs by bulk copies:
+// one thread of the tile issues the loads (the W columns of a COL tile are one
+// run; a MIX tile's two columns are two), every thread of the tile waits on the
+// tile's mbarrier, and after the updates the same thread writes the runs back
+// with bulk stores. Otherwise every thread copies elements with cp.async.
 //
 // CT: a whole CTA shares one tile (its threads split each term's entries, a CTA
 // barrier between terms); otherwise every warp owns its own tile.
@@ -47,6 +93,7 @@ template <typename R, class A, int PT, bool CT>
 __global__ void k_pass(PassLaunch pl) {
   using C2 = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[CT ? 1 : 32];  // one mbarrier per tile slot (bulk copies)
   const uint32_t lane = CT ? threadIdx.x : (threadIdx.x & 31);  // thread index within the tile
   const uint32_t tpt = CT ? blockDim.x : 32u;                    // threads per tile
   const uint32_t warp = CT ? 0u : (threadIdx.x >> 5);            // tile slot within the CTA
@@ -58,6 +105,16 @@ __global__ void k_pass(PassLaunch pl) {
   const uint32_t logW = __ffs(W) - 1;
   C2* __restrict__ st = reinterpret_cast<C2*>(smem_raw) + (size_t)warp * L * W;
   const uint32_t* __restrict__ pool = pl.pool;
+  const bool bulk = PT != PASS_ROW && pl.bulk != 0;
+  const uint32_t bar = static_cast<uint32_t>(__cvta_generic_to_shared(&bars[warp]));
+  if (bulk) {
+    if (lane == 0) {
+      mbar_init1(bar);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+  }
+  uint32_t phase = 0;
   uint32_t ntiles;
   if (PT == PASS_COL) ntiles = (Cb + W - 1) >> logW;
   else if (PT == PASS_ROW) ntiles = Ca;
@@ -77,24 +134,48 @@ __global__ void k_pass(PassLaunch pl) {
       parb = x.x >> 31;
     }
     const uint32_t nl = (PT == PASS_COL) ? min(W, Cb - b0) : W;  // valid lines
-    // Element i of the stage <-> block offset g(i). The gather is a stream of
-    // asynchronous global -> shared copies (cp.async), all in flight at once, so
-    // a tile pays the L2 latency once rather than once per element.
-    auto goff = [&](uint32_t i) -> uint64_t {
-      const uint32_t e = i >> logW, w = i & (W - 1);
-      if (PT == PASS_COL) return (uint64_t)(b0 + w) * Ca + e;
-      if (PT == PASS_ROW) return (uint64_t)e * Ca + row;
-      return (uint64_t)(w ? b10 : b01) * Ca + e;
-    };
-    const uint32_t nst = L * W;
-    for (uint32_t i = lane; i < nst; i += tpt)
-      if ((i & (W - 1)) < nl) async_copy(st + i, blk + goff(i));
-    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+    // The tile's runs of the working block: line w of the stage is Ca (or, for a
+    // row, Cb) elements from column col(w) on (a row: strided, element-wise).
+    auto col = [&](uint32_t w) -> uint32_t { return PT == PASS_COL ? b0 + w : (w ? b10 : b01); };
+    if (bulk) {
+      if (lane == 0) {
+        const uint32_t bytes = Ca * (uint32_t)sizeof(C2);
+        mbar_arrive_tx(bar, nl * bytes);
+        if (PT == PASS_COL) {
+          bulk_load(st, blk + (uint64_t)b0 * Ca, nl * bytes, bar);
+        } else {
+          bulk_load(st, blk + (uint64_t)b01 * Ca, bytes, bar);
+          bulk_load(st + Ca, blk + (uint64_t)b10 * Ca, bytes, bar);
+        }
+      }
+      bool ok = mbar_wait_bounded(bar, phase);
+      ok = CT ? (__syncthreads_and(ok) != 0) : (__all_sync(0xffffffffu, ok) != 0);  // one verdict per tile
+      if (!ok) {
+        // the copies did not complete: record it, give the copies in flight one
+        // more bounded wait, and stop (the pass's results are invalid)
+        if (lane == 0) {
+          atomicOr(pl.err, kPassErrWait);
+          mbar_wait_bounded(bar, phase);
+        }
+        break;
+      }
+      phase ^= 1u;
+    } else {
+      // all of the tile's element copies in flight at once (cp.async), so the
+      // tile pays the L2 latency once rather than once per element
+      if (PT == PASS_ROW) {
+        for (uint32_t e = lane; e < L; e += tpt) async_copy(st + e, blk + (uint64_t)e * Ca + row);
+      } else {
+        for (uint32_t w = 0; w < nl; ++w)
+          for (uint32_t e = lane; e < Ca; e += tpt) async_copy(st + w * Ca + e, blk + (uint64_t)col(w) * Ca + e);
+      }
+      asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+    }
     Sync()();
     if (PT == PASS_MIX) {
       chunked_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, lane, tpt, true, parb,
-                            [&](uint32_t a) -> C2& { return st[2 * a]; },
-                            [&](uint32_t a) -> C2& { return st[2 * a + 1]; }, icoef, Sync());
+                            [&](uint32_t a) -> C2& { return st[a]; }, [&](uint32_t a) -> C2& { return st[Ca + a]; },
+                            icoef, Sync());
     } else {
       // Lane l owns line l % W and walks entries l / W, l / W + 32 / W, ...
       const uint32_t w = lane & (W - 1);
@@ -102,13 +183,35 @@ __global__ void k_pass(PassLaunch pl) {
       const uint32_t line = (PT == PASS_COL) ? b0 + w : row;
       const uint32_t lstr = active ? __ldg(((PT == PASS_COL) ? pl.strB : pl.strA) + line) : 0u;
       chunked_line_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, L, lane >> logW,
-                             tpt >> logW, active, lstr, [&](uint32_t e) -> C2& { return st[(e << logW) + w]; }, icoef,
+                             tpt >> logW, active, lstr, [&](uint32_t e) -> C2& { return st[w * L + e]; }, icoef,
                              Sync());
     }
-    for (uint32_t i = lane; i < nst; i += tpt)
-      if ((i & (W - 1)) < nl) blk[goff(i)] = st[i];
+    if (bulk) {
+      // the updates (generic proxy) must be visible to the bulk copy (async proxy)
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      Sync()();
+      if (lane == 0) {
+        const uint32_t bytes = Ca * (uint32_t)sizeof(C2);
+        if (PT == PASS_COL) {
+          bulk_store(blk + (uint64_t)b0 * Ca, st, nl * bytes);
+        } else {
+          bulk_store(blk + (uint64_t)b01 * Ca, st, bytes);
+          bulk_store(blk + (uint64_t)b10 * Ca, st + Ca, bytes);
+        }
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        // the stage is read before the next tile's loads overwrite it
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+      }
+    } else if (PT == PASS_ROW) {
+      for (uint32_t e = lane; e < L; e += tpt) blk[(uint64_t)e * Ca + row] = st[e];
+    } else {
+      for (uint32_t w = 0; w < nl; ++w)
+        for (uint32_t e = lane; e < Ca; e += tpt) blk[(uint64_t)col(w) * Ca + e] = st[w * Ca + e];
+    }
     Sync()();
   }
+  // the bulk stores are complete (in global memory) before the CTA exits
+  if (bulk && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 size_t pass_stage_elems(const Pass& pass, uint32_t Ca, uint32_t Cb, uint32_t W) {

@@ -54,7 +54,15 @@ struct PassLaunch {
   // > 0: one tile per CTA of this many threads (a multiple of 32), which split
   // every term's entries (long tables); 0: one tile per warp.
   uint32_t cta_tile;
+  // 1: column and column-pair tiles move between the working block and shared
+  // memory as whole columns by bulk copies (cp.async.bulk, completing on an
+  // mbarrier); needs every column to start on a 16-byte boundary (Ca * element
+  // size a multiple of 16, working blocks 16-byte aligned).
+  uint32_t bulk;
+  // Device error word: a bounded wait that runs out ORs in kPassErrWait.
+  int* err;
 };
+constexpr int kPassErrWait = 2;
 constexpr uint32_t kCtaTileThreads = 128;
 size_t pass_stage_elems(const Pass& pass, uint32_t Ca, uint32_t Cb, uint32_t W);
 cudaError_t launch_pass(const PassLaunch& pl, int dtype, cudaStream_t s);

@@ -208,6 +208,30 @@ def diagonal_features(hamiltonian, strings: np.ndarray) -> np.ndarray:
     return np.stack([np.minimum(z, 8.0), np.exp(-z)], axis=1).astype(np.float32)
 
 
+def lowest_diagonal_state(hamiltonian, strings: np.ndarray) -> np.ndarray:
+    """The determinant of lowest diagonal energy <x|H|x> (a classical start that
+    needs no training), as a normalised state over `strings`."""
+    e = diagonal_energies(hamiltonian, strings)
+    psi = np.zeros(len(strings), np.complex128)
+    psi[int(np.argmin(e))] = 1.0
+    return psi
+
+
+def variational_energy(program_tau, psi: np.ndarray, tau: float, device: int = 0) -> float:
+    """<psi|H|psi> from one short evolution on the GPU: program_tau is the
+    Hamiltonian's program at a small timestep tau (one first-order step), and
+    <psi|U(tau)|psi> = exp(-i <H> tau) (1 + O(tau^2)), so <H> = -arg(...) / tau up
+    to O(tau^2). Used to choose between two starts without knowing the answer."""
+    from .time_evolution import DeviceState
+    psi = np.asarray(psi, np.complex128)
+    psi = psi / np.linalg.norm(psi)
+    st = DeviceState(program_tau.num_orbitals, program_tau.n_alpha, program_tau.n_beta, 1, device=device)
+    st.upload(psi)
+    st.evolve(program_tau)
+    u = st.download(first=len(psi), count=len(psi))
+    return float(-np.angle(np.vdot(psi, u)) / tau)
+
+
 def proposed_state(model: AmplitudeMLP, strings: np.ndarray, feats=None) -> np.ndarray:
     """The model's state over `strings` (with the features of their Hamiltonian
     when the model takes features), normalised to 1."""

@@ -884,6 +884,24 @@ def run_learned(args, w, rank, ws, local):
     }
 
 
+FORMS = ("precision-n24", "batched-256")
+
+
+def run_forms(args, rank, ws, local):
+    """The precision and batching forms, run after the headline workload in the
+    same command, each with its own line (value, e2e, roofline, cpu_baseline,
+    precision_check; per_size for the batch). They time min(steps, 5) steps after
+    3 warm-up steps, so that the default run stays within minutes."""
+    out = {}
+    for name in FORMS:
+        a = argparse.Namespace(**vars(args))
+        a.workload, a.steps, a.warmup = name, min(args.steps, 5), 3
+        a.strategy, a.cluster, a.powers, a.precision = 0, 0, 0, 0
+        fw = dict(WORKLOADS[name])
+        out[name] = run_batch(a, fw, rank, ws, local) if fw.get("batch") else run_ours(a, fw, rank, ws, local)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -900,6 +918,8 @@ def main():
                     help="evolve only the first K controlled powers (profiling runs; not a workload's figure)")
     ap.add_argument("--precision", type=int, default=0,
                     help="override the ancilla count (profiling runs on a smaller register; not a workload's figure)")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="with the default workload, skip the nested precision and batching forms")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -916,6 +936,9 @@ def main():
         line = run_batch(args, w, rank, ws, local)
     else:
         line = run_ours(args, w, rank, ws, local)
+        if (args.workload == DEFAULT_WORKLOAD and not args.no_forms and not args.powers and not args.precision
+                and not args.strategy):
+            line["forms"] = run_forms(args, rank, ws, local)
     if rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
     if ws > 1 and args.impl == "ours":

@@ -80,7 +80,7 @@ int qpe_timer_elapsed_ms(qpe_context* ctx, uint32_t start_slot, uint32_t end_slo
 
 /* Measures the device's FP64 FMA throughput (TFLOP/s, an FMA counting 2): a
  * kernel of 8 independent FMA chains per thread on 4 x 256-thread CTAs per SM,
- * timed with CUDA events on the context's stream (slots 14 and 15). A
+ * timed with CUDA events of its own on the context's stream. A
  * measurement helper for reporting FP64 roofline fractions; no counterpart in
  * the reference. */
 int qpe_measure_fp64_peak(qpe_context* ctx, double* tflops);

@@ -467,3 +467,13 @@ def test_autotune_leaves_register_unchanged(gpu):
     ref.upload(reg)
     ref.evolve_in_place(prog2, 1, 2, strategy=3)
     assert np.array_equal(st.download(), ref.download())
+
+
+def test_fp64_peak_probe(gpu):
+    """qpe_measure_fp64_peak (the FP64 roofline denominator the bench reports)
+    returns a plausible FMA rate for one GPU."""
+    import ctypes
+    N = gpu._native
+    v = ctypes.c_double()
+    N.check(N.lib().qpe_measure_fp64_peak(N.context(0), ctypes.byref(v)))
+    assert 0.1 < v.value < 200.0, v.value
