@@ -232,6 +232,68 @@ def variational_energy(program_tau, psi: np.ndarray, tau: float, device: int = 0
     return float(-np.angle(np.vdot(psi, u)) / tau)
 
 
+def lowest_diagonal_state(hamiltonian, strings: np.ndarray) -> np.ndarray:
+    """The determinant of lowest diagonal energy <x|H|x> (a classical start that
+    needs no training), as a normalised state over `strings`."""
+    e = diagonal_energies(hamiltonian, strings)
+    psi = np.zeros(len(strings), np.complex128)
+    psi[int(np.argmin(e))] = 1.0
+    return psi
+
+
+def variational_energy(program_tau, psi: np.ndarray, tau: float, device: int = 0) -> float:
+    """<psi|H|psi> from one short evolution on the GPU: program_tau is the
+    Hamiltonian's program at a small timestep tau (one first-order step), and
+    <psi|U(tau)|psi> = exp(-i <H> tau) (1 + O(tau^2)), so <H> = -arg(...) / tau up
+    to O(tau^2). Used to choose between starts without knowing the answer."""
+    from .time_evolution import DeviceState
+    psi = np.asarray(psi, np.complex128)
+    psi = psi / np.linalg.norm(psi)
+    st = DeviceState(program_tau.num_orbitals, program_tau.n_alpha, program_tau.n_beta, 1, device=device)
+    st.upload(psi)
+    st.evolve(program_tau)
+    u = st.download(first=len(psi), count=len(psi))
+    return float(-np.angle(np.vdot(psi, u)) / tau)
+
+
+def variational_energies(programs_tau, states, tau: float, device: int = 0) -> np.ndarray:
+    """variational_energy for many (program, state) pairs in one batched launch:
+    a batch of one controlled power (P = 1) per pair, complex128. The batch's QIFT
+    turns blocks (b0, b1) into ((b0 + b1) / sqrt 2, (b0 - b1) / sqrt 2), so
+    b1 = U(tau) psi is recovered from the two blocks it returns."""
+    from .batching import Batch
+    states = [np.asarray(x, np.complex128) / np.linalg.norm(x) for x in states]
+    bt = Batch(list(programs_tau), 1, dtype=np.complex128, device=device)
+    for i, x in enumerate(states):
+        bt.upload(i, x)
+    bt.run()
+    out = np.zeros(len(states))
+    for i, x in enumerate(states):
+        r = bt.download(i)
+        d = len(x)
+        u = (r[:d] - r[d:]) / np.sqrt(2.0)
+        out[i] = -np.angle(np.vdot(x, u)) / tau
+    return out
+
+
+def truncated(psi: np.ndarray, m: int) -> np.ndarray:
+    """psi restricted to its m largest amplitudes, renormalised."""
+    psi = np.asarray(psi, np.complex128)
+    keep = np.argsort(-np.abs(psi))[:m]
+    out = np.zeros_like(psi)
+    out[keep] = psi[keep]
+    return out / np.linalg.norm(out)
+
+
+# The model's candidate starts: its whole proposed state and the proposal cut
+# to its m largest amplitudes; variational energy picks one of them.
+CANDIDATE_TRUNCATIONS = (1, 2, 4, 8, 16, 64, 256)
+
+
+def learned_candidates(psi: np.ndarray) -> list:
+    return [psi] + [truncated(psi, m) for m in CANDIDATE_TRUNCATIONS if m < len(psi)]
+
+
 def proposed_state(model: AmplitudeMLP, strings: np.ndarray, feats=None) -> np.ndarray:
     """The model's state over `strings` (with the features of their Hamiltonian
     when the model takes features), normalised to 1."""
@@ -249,6 +311,38 @@ def ground_bin(probs: np.ndarray, t_power: float, rel: float = 0.02) -> int:
     thr = rel * float(probs.max())
     cand = [j for j in range(n) if probs[j] >= thr and probs[j] >= probs[(j - 1) % n] and probs[j] >= probs[(j + 1) % n]]
     return int(min(cand, key=lambda j: phase_to_energy(j / n, t_power)))
+
+
+def shared_ground_bin(hists, t_power: float, rel: float = 1e-3) -> int:
+    """The ground bin of one Hamiltonian from several QPE histograms (one per
+    start): the lowest-energy bin that is a local maximum holding at least `rel`
+    of the probability in at least one of them. The same bin then scores every
+    start, so no start's own peak shape decides the target."""
+    from .readout import phase_to_energy
+    cand = set()
+    for p in hists:
+        p = np.asarray(p, np.float64)
+        n = len(p)
+        thr = rel * float(p.sum())
+        cand |= {j for j in range(n) if p[j] >= thr and p[j] >= p[(j - 1) % n] and p[j] >= p[(j + 1) % n]}
+    n = len(hists[0])
+    return int(min(cand, key=lambda j: phase_to_energy(j / n, t_power)))
+
+
+def qpe_time_to_precision(success: float, seconds_per_power: float, t_power: float, tol: float = 1e-3,
+                          confidence: float = 0.9):
+    """Time for textbook QPE to resolve the ground energy to `tol` from a start
+    whose runs land in the ground window with probability `success`: a register
+    of bits = ceil(log2(2 pi / (t_power * 2 tol))) ancilla qubits (bins at most
+    2 tol wide), 2^bits - 1 controlled powers per run at `seconds_per_power`, and
+    runs = ceil(log(1 - confidence) / log(1 - success)) so that the ground window
+    is observed at least once with that confidence. Returns (seconds, runs,
+    bits); seconds is None when success is 0."""
+    bits = int(math.ceil(math.log2(2.0 * math.pi / (t_power * 2.0 * tol))))
+    if success <= 0.0:
+        return None, None, bits
+    runs = 1 if success >= 1.0 else int(math.ceil(math.log(1.0 - confidence) / math.log1p(-success)))
+    return runs * ((1 << bits) - 1) * seconds_per_power, runs, bits
 
 
 def window_mass(probs: np.ndarray, j0: int, half: int = 1) -> float:

@@ -78,18 +78,19 @@ WORKLOADS["batched-32"] = dict(WORKLOADS["batched-256"], count=32,
                                desc="Batching form, 32-instance draw (profiling case): n uniform in "
                                     "{12,14,16,18,20}, N=n/2, 6 ancilla qubits, complex64, dt=0.05")
 # The learned initial-state form: n = 20, N = 10.
-WORKLOADS["learned-n20"] = dict(learned=True, n=20, N=10, P=10, P_data=6, dt=0.05, train=512, held_out=64,
+WORKLOADS["learned-n20"] = dict(learned=True, n=20, N=10, P=10, P_data=8, dt=0.05, tau=1e-3, train=512, held_out=64,
                                 train_steps=3000, batch=65536, lr=1e-3, seed=31337, dtype="c64",
                                 desc="Learned initial state: n=20, N=10 (63,504 amplitudes per block in the "
                                      "reference's Na=Nb layout), 10 ancilla qubits for evaluation; MLP (20 occupation "
                                      "bits + 2 diagonal-energy features of the string under its Hamiltonian) -> 3 x 256 "
                                      "GELU -> (log|a|, phase), BF16 tensor-core training on the post-selected ground "
-                                     "projections of 512 seeded Hamiltonians (QPE with 6 ancilla qubits, complex64), "
-                                     "evaluated on 64 held-out seeds against Hartree-Fock")
+                                     "projections of 512 seeded Hamiltonians (QPE with 8 ancilla qubits from each "
+                                     "Hamiltonian's lowest-diagonal determinant, complex64), evaluated on 64 held-out "
+                                     "seeds against Hartree-Fock")
 # A small draw of the same form (n=12) for quick checks of the pipeline.
-WORKLOADS["learned-n12"] = dict(WORKLOADS["learned-n20"], n=12, N=6, P=8, train=32, held_out=8, train_steps=300,
-                                batch=8192, desc="Learned initial state, small check: n=12, N=6, 32 training and "
-                                                 "8 held-out seeds, 8 ancilla qubits")
+WORKLOADS["learned-n12"] = dict(WORKLOADS["learned-n20"], n=12, N=6, P=8, train=64, held_out=16, train_steps=600,
+                                batch=8192, desc="Learned initial state, small check: n=12, N=6, 64 training and "
+                                                 "16 held-out seeds, 8 ancilla qubits")
 DEFAULT_WORKLOAD = "plain-n16"
 
 # DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum +
@@ -749,55 +750,59 @@ def run_reference(args, w, rank, ws):
 
 
 def run_learned(args, w, rank, ws, local):
-    """The learned-state form end to end: post-selected ground projections of the
-    training Hamiltonians (batched QPE on the GPU), BF16 tensor-core training,
-    then QPE from Hartree-Fock and from the learned state on held-out
-    Hamiltonians. Per held-out Hamiltonian: ground-state overlap (with the
-    post-selected ground projection of a P-qubit QPE run), success probability
-    (mass of the ground bin and its neighbours) and the time to a 1e-3 Ha
-    estimate (QPE shots needed by the sub-bin estimator, simulated from the
-    exact histogram, divided by the success rate, times the GPU time per run).
-    Hartree-Fock is kept wherever the proposal loses."""
+    """The learned-state form end to end.
+
+    1. Training data from the simulator itself: a batched QPE run (complex64,
+       P_data ancilla qubits) of every training Hamiltonian from its determinant
+       of lowest diagonal energy; the histogram's lowest-energy peak picks the
+       ground bin and that block of the QIFT'd register, normalised, is the
+       post-selected ground projection.
+    2. BF16 training of the model on the tensor cores.
+    3. The learned start of every held-out Hamiltonian, chosen without the
+       answer: the model proposes its state and cuts of it to its m largest
+       amplitudes (learned_candidates); the lowest variational energy among them
+       (one short GPU evolution each, all in one batched launch) is the learned
+       start, which is run if its energy is below Hartree-Fock's; Hartree-Fock
+       stays the fallback whenever the proposal loses.
+    4. One batched QPE run (P ancilla qubits) per held-out Hamiltonian from four
+       starts: Hartree-Fock, the learned start, the lowest-diagonal determinant
+       (a classical reference that needs no training) and the model's uncut
+       proposal. The ground bin is the lowest-energy peak over the four
+       histograms; success is each start's mass in that bin +- 1; the overlap is
+       with the post-selected ground projection of the start with the largest
+       success; the time to 1e-3 Ha is the textbook QPE cost
+       (qpe_time_to_precision) at the measured GPU time per controlled power."""
     q = graft.load_package()
     N = q._native
     L = q.learned_state
     M, na, nb = w["n"] // 2, w["N"] // 2, w["N"] - w["N"] // 2
-    dt, Pd, P = w["dt"], w["P_data"], w["P"]
+    dt, Pd, P, tau = w["dt"], w["P_data"], w["P"], w["tau"]
     strings = L.register_strings(M, na, nb)
     ld = len(strings)
     timer = N.Timer(local)
 
-    def programs(seeds):
-        """Programs of the seeds' Hamiltonians and the model's features of every string under each."""
-        out, feats = [], []
-        for s in seeds:
-            h = q.Hamiltonian.from_integrals(q.synthetic_integrals(w["n"], s), na, dt)
-            out.append(q.Program(h.segmented_terms(), M, na, nb, device=local))
-            feats.append(L.diagonal_features(h, strings))
-        return out, feats
+    def hams(seeds, t):
+        return [q.Hamiltonian.from_integrals(q.synthetic_integrals(w["n"], s), na, t) for s in seeds]
 
     base = w["seed"] + 100000 * rank
     train_seeds = [base + i for i in range(w["train"])]
     eval_seeds = [base + 50000 + i for i in range(w["held_out"])]
     t0 = time.perf_counter()
     # 1. post-selected ground projections of the training Hamiltonians
-    progs, tfeats = programs(train_seeds)
+    th = hams(train_seeds, dt)
+    progs = [q.Program(h.segmented_terms(), M, na, nb, device=local) for h in th]
+    tfeats = [L.diagonal_features(h, strings) for h in th]
     bt = q.Batch(progs, Pd, dtype=np.complex64, device=local)
-    hf = q.hf_block0(math.comb(M, na), math.comb(M, nb), Pd, np.complex64)
-    for i in range(len(progs)):
-        bt.upload(i, hf)
+    for i, h in enumerate(th):
+        bt.upload(i, (L.lowest_diagonal_state(h, strings) * 2.0 ** (-Pd / 2)).astype(np.complex64))
     timer.record(0)
     bt.run()
     timer.record(1)
     data_ms = timer.elapsed_ms(0, 1)
-    bits, la, ph, wt = [], [], [], []
-    nd = 1 << Pd
+    la, ph, wt = [], [], []
     for i in range(len(progs)):
-        pr = bt.phase_probs(i)
-        j0 = L.ground_bin(pr, dt)
-        blk = bt.download(i, first=j0 * ld, count=ld)
-        a, b, c = L.state_targets(blk)
-        bits.append(strings)
+        j0 = L.ground_bin(bt.phase_probs(i), dt)
+        a, b, c = L.state_targets(bt.download(i, first=j0 * ld, count=ld))
         la.append(a)
         ph.append(b)
         wt.append(c)
@@ -805,82 +810,125 @@ def run_learned(args, w, rank, ws, local):
     data_s = time.perf_counter() - t0
     # 2. training on the tensor cores
     model = L.AmplitudeMLP(w["n"], batch=w["batch"], seed=w["seed"], device=local, n_feat=L.N_DIAG_FEATURES)
-    model.set_data(np.concatenate(bits), np.concatenate(la), np.concatenate(ph), np.concatenate(wt),
+    model.set_data(np.concatenate([strings] * len(th)), np.concatenate(la), np.concatenate(ph), np.concatenate(wt),
                    np.concatenate(tfeats))
     model.train(20, lr=w["lr"], seed=1)  # warm-up
     t1 = time.perf_counter()
     losses = model.train(w["train_steps"], lr=w["lr"], seed=2)
     train_s = time.perf_counter() - t1
     tflops = model.tensor_flops_per_step() * w["train_steps"] / train_s / 1e12
-    # 3. evaluation: QPE from HF and from the learned state on held-out Hamiltonians
-    eprogs, efeats = programs(eval_seeds)
-    bt = q.Batch(eprogs + eprogs, P, dtype=np.complex64, device=local)
-    hfP = q.hf_block0(math.comb(M, na), math.comb(M, nb), P, np.complex64)
+    # 3. the starts of every held-out Hamiltonian and the choice without the answer
+    eh = hams(eval_seeds, dt)
+    eprogs = [q.Program(h.segmented_terms(), M, na, nb, device=local) for h in eh]
+    ptau = [q.Program(h.segmented_terms(), M, na, nb, device=local) for h in hams(eval_seeds, tau)]
+    H = len(eh)
+    t2 = time.perf_counter()
+    psi_hf = np.zeros(ld, np.complex128)
+    psi_hf[0] = 1.0
+    diags = [L.lowest_diagonal_state(h, strings) for h in eh]
+    fulls, cands, owner, flat = [], [], [], []
+    for i, h in enumerate(eh):
+        full = L.proposed_state(model, strings, L.diagonal_features(h, strings))
+        fulls.append(full)
+        c = L.learned_candidates(full)
+        cands.append(c)
+        for x in [psi_hf, diags[i]] + c:
+            owner.append(i)
+            flat.append(x)
+    ev_flat = L.variational_energies([ptau[o] for o in owner], flat, tau, device=local)
+    choose_s = (time.perf_counter() - t2) / H
+    starts, evar, picked = [], [], []
+    pos = 0
+    for i in range(H):
+        k = len(cands[i])
+        e_hf, e_dg, e_c = ev_flat[pos], ev_flat[pos + 1], ev_flat[pos + 2:pos + 2 + k]
+        pos += 2 + k
+        sel = int(np.argmin(e_c))
+        picked.append(0 if sel == 0 else L.CANDIDATE_TRUNCATIONS[sel - 1])
+        starts.append((psi_hf, cands[i][sel], diags[i], fulls[i]))
+        evar.append((float(e_hf), float(e_c[sel]), float(e_dg), float(e_c[0])))
+    # 4. QPE from the four starts in one batched launch
+    names = ("hf", "learned", "diagonal", "learned_full")
+    ns = len(names)
+    bt = q.Batch(eprogs * ns, P, dtype=np.complex64, device=local)
     scale = 2.0 ** (-P / 2)
-    # the model's state for each held-out Hamiltonian (its features differ per Hamiltonian)
-    learned_states = [L.proposed_state(model, strings, efeats[i]) for i in range(len(eprogs))]
-    for i in range(len(eprogs)):
-        bt.upload(i, hfP)
-        bt.upload(len(eprogs) + i, (learned_states[i] * scale).astype(np.complex64))
+
+    def upload_starts():
+        for k in range(ns):
+            for i in range(H):
+                bt.upload(k * H + i, (starts[i][k] * scale).astype(np.complex64))
+
+    upload_starts()
     bt.run()  # warm-up of the graph
-    for i in range(len(eprogs)):
-        bt.upload(i, hfP)
-        bt.upload(len(eprogs) + i, (learned_states[i] * scale).astype(np.complex64))
+    upload_starts()
     timer.record(2)
     bt.run()
     timer.record(3)
     eval_ms = timer.elapsed_ms(2, 3)
-    t_run = eval_ms / 1e3 / (2 * len(eprogs))  # GPU seconds per QPE run, batched
+    sec_per_power = eval_ms / 1e3 / (ns * H * ((1 << P) - 1))  # one instance's power, batched
     rows = []
-    for i in range(len(eprogs)):
-        p_hf, p_l = bt.phase_probs(i), bt.phase_probs(len(eprogs) + i)
-        j0 = L.ground_bin(p_hf, dt)
-        g = bt.download(i, first=j0 * ld, count=ld).astype(np.complex128)
+    for i in range(H):
+        hists = [bt.phase_probs(k * H + i) for k in range(ns)]
+        j0 = L.shared_ground_bin(hists, dt)
+        succ = [L.window_mass(p, j0) for p in hists]
+        best = int(np.argmax(succ))
+        g = bt.download(best * H + i, first=j0 * ld, count=ld).astype(np.complex128)
         g /= np.linalg.norm(g)
-        e_t = L.subbin_energy(p_hf / p_hf.sum(), j0, 1 << P, dt)
-        psi_hf = np.zeros(ld, np.complex128)
-        psi_hf[0] = 1.0
-        ov_hf = float(abs(np.vdot(g, psi_hf)) ** 2)
-        ov_l = float(abs(np.vdot(g, learned_states[i])) ** 2)
-        s_hf, s_l = L.window_mass(p_hf, j0), L.window_mass(p_l, j0)
-        n_hf = L.shots_to_precision(p_hf, j0, dt, e_t, seed=i)
-        n_l = L.shots_to_precision(p_l, j0, dt, e_t, seed=i)
-        t_hf = n_hf * t_run / max(s_hf, 1e-300) if n_hf else None
-        t_l = n_l * t_run / max(s_l, 1e-300) if n_l else None
-        use_l = t_l is not None and (t_hf is None or t_l < t_hf)
-        rows.append(dict(overlap_hf=ov_hf, overlap_learned=ov_l, success_hf=s_hf, success_learned=s_l,
-                         time_hf=t_hf, time_learned=t_l, time_chosen=t_l if use_l else t_hf, learned_wins=use_l))
+        ov = [float(abs(np.vdot(g, starts[i][k])) ** 2) for k in range(ns)]
+        tt = [L.qpe_time_to_precision(sc, sec_per_power, dt)[0] for sc in succ]
+        use_l = evar[i][1] < evar[i][0]
+        r = {f"{nm}_{key}": v for key, vals in (("overlap", ov), ("success", succ), ("time_s", tt),
+                                                ("energy_var", evar[i])) for nm, v in zip(names, vals)}
+        r["learned_chosen"] = use_l
+        r["chosen_time_s"] = tt[1] if use_l else tt[0]
+        r["chosen_no_slower"] = tt[0] is None or (r["chosen_time_s"] is not None and r["chosen_time_s"] <= tt[0])
+        rows.append(r)
     del bt
 
     def med(key):
         v = [r[key] for r in rows if r[key] is not None]
         return statistics.median(v) if v else None
 
-    value = med("time_chosen")
+    gain = [r["hf_time_s"] / r["chosen_time_s"] for r in rows if r["hf_time_s"] and r["chosen_time_s"]]
+    value = med("chosen_time_s")
     peaks_d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     bf16_peak = float(peaks_d.get("bf16_tflops", 1900.0))
+    bits = L.qpe_time_to_precision(0.5, sec_per_power, dt)[2]
     return {
         "metric": "time to 1e-3 Ha QPE, learned (Hartree-Fock fallback) vs Hartree-Fock", "value": value, "unit": "s",
         "n_gpus": ws, "steps": 1, "warmup": 1, "ms_per_step": eval_ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 model, complex64 register",
-        "data": "synthetic: seeded integrals, 512 training and 64 held-out seeds",
+        "data": f"synthetic: seeded integrals, {w['train']} training and {w['held_out']} held-out seeds",
         "config": {"workload": args.workload, "description": w["desc"], "train_hamiltonians": w["train"],
-                   "held_out": w["held_out"], "precision": P, "precision_data": Pd, "dt": dt,
+                   "held_out": w["held_out"], "precision": P, "precision_data": Pd, "dt": dt, "tau": tau,
                    "train_steps": w["train_steps"], "batch": w["batch"], "lr": w["lr"]},
-        "learned": {"median_time_hf_s": med("time_hf"), "median_time_learned_s": med("time_learned"),
-                    "median_overlap_hf": med("overlap_hf"), "median_overlap_learned": med("overlap_learned"),
-                    "median_success_hf": med("success_hf"), "median_success_learned": med("success_learned"),
-                    "learned_wins": int(sum(r["learned_wins"] for r in rows)), "held_out": len(rows),
-                    "reached_1e-3_hf": int(sum(r["time_hf"] is not None for r in rows)),
-                    "reached_1e-3_learned": int(sum(r["time_learned"] is not None for r in rows)),
-                    "gpu_seconds_per_qpe_run": t_run, "loss_first": float(losses[:10].mean()),
-                    "loss_last": float(losses[-10:].mean()), "data_generation_s": data_s,
-                    "data_qpe_gpu_ms": data_ms, "training_s": train_s},
-        "roofline": {"bound": "tensor", "achieved": tflops, "peak": bf16_peak, "unit": "TFLOP/s",
+        "learned": {"median_time_hf_s": med("hf_time_s"), "median_time_learned_s": med("learned_time_s"),
+                    "median_time_diagonal_s": med("diagonal_time_s"), "median_time_chosen_s": value,
+                    "median_speedup_chosen_over_hf": statistics.median(gain) if gain else None,
+                    "median_overlap_hf": med("hf_overlap"), "median_overlap_learned": med("learned_overlap"),
+                    "median_overlap_diagonal": med("diagonal_overlap"),
+                    "median_overlap_learned_full": med("learned_full_overlap"),
+                    "median_success_hf": med("hf_success"), "median_success_learned": med("learned_success"),
+                    "median_success_diagonal": med("diagonal_success"),
+                    "median_success_learned_full": med("learned_full_success"),
+                    "learned_cut_picked": {str(m): int(sum(1 for x in picked if x == m)) for m in sorted(set(picked))},
+                    "learned_chosen": int(sum(r["learned_chosen"] for r in rows)), "held_out": len(rows),
+                    "learned_beats_hf_success": int(sum(r["learned_success"] > r["hf_success"] for r in rows)),
+                    "learned_beats_diagonal_success": int(sum(r["learned_success"] > r["diagonal_success"]
+                                                              for r in rows)),
+                    "chosen_no_slower_than_hf": int(sum(r["chosen_no_slower"] for r in rows)),
+                    "qpe_bits_for_1e-3_ha": bits, "gpu_seconds_per_power": sec_per_power,
+                    "choice_seconds_per_hamiltonian": choose_s,
+                    "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-10:].mean()),
+                    "data_generation_s": data_s, "data_qpe_gpu_ms": data_ms, "training_s": train_s},
+        "roofline": {"bound": "latency", "achieved": tflops, "peak": bf16_peak, "unit": "TFLOP/s",
                      "frac": tflops / bf16_peak, "traffic": None,
-                     "kernel": "k_gemm (tcgen05 BF16, training step of 11 GEMMs + elementwise kernels)"},
-        "target": "sub-bin estimate of the noiseless P-qubit histogram from Hartree-Fock (the Trotterised "
-                  "ground-state phase the QPE measures)",
+                     "kernel": "k_gemm (tcgen05 BF16, a training step of 11 GEMMs of a 150k-parameter model plus "
+                               "elementwise kernels)",
+                     "bound_note": "each GEMM of the small model is a few microseconds of tensor work; a step is "
+                                   "bound by its chain of dependent launches"},
+        "target": "the ground bin shared by the four starts' histograms; overlap with the post-selected ground "
+                  "projection of the start with the largest success; time from the textbook QPE cost model",
     }
 
 
