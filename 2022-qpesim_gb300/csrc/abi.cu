@@ -107,6 +107,69 @@ static void state_alloc(qpe_state* st) {
   QPE_CK(configure_qift_kernels(st->dtype, qift_smem_bytes(st->P, st->qift_T, st->dtype)));
 }
 
+// The image of every MIX pass whose descriptors and tables fit in
+// kPassImageMaxBytes: the pass's DevOps with `tab` rewritten to a word offset in
+// the image, then each table they use once, every region starting on a 16-byte
+// boundary. The descriptors are written here; the tables, which only exist on
+// the device, are copied in from the index pool by k_copy_segments.
+static void build_pass_images(qpe_program* pr) {
+  const HostProgram& hp = pr->hp;
+  pr->img_off.assign(hp.passes.size(), 0);
+  pr->img_words.assign(hp.passes.size(), 0);
+  std::vector<uint32_t> host;
+  std::vector<PassImageSeg> segs;
+  auto round4 = [](uint64_t w) { return (w + 3) & ~(uint64_t)3; };
+  for (size_t pi = 0; pi < hp.passes.size(); ++pi) {
+    const Pass& p = hp.passes[pi];
+    if (p.type != PASS_MIX || p.op1 <= p.op0) continue;
+    const uint32_t n = p.op1 - p.op0;
+    std::vector<std::pair<uint32_t, uint32_t>> region;  // (pool word, image word)
+    uint64_t words = (uint64_t)n * (sizeof(DevOp) / 4);
+    bool ok = true;
+    for (uint32_t i = 0; i < n && ok; ++i) {
+      const DevOp& d = hp.ops[p.op0 + i];
+      if (d.kind != OPK_PAIR) ok = false;
+      bool seen = false;
+      for (const auto& r : region) seen = seen || r.first == d.tab;
+      if (!seen) {
+        region.push_back({d.tab, (uint32_t)words});
+        words = round4(words + 2ull * d.count);
+      }
+    }
+    words = round4(words);
+    if (!ok || words * 4 > kPassImageMaxBytes) continue;
+    const size_t base = host.size();
+    host.resize(base + words, 0u);
+    for (uint32_t i = 0; i < n; ++i) {
+      DevOp e = hp.ops[p.op0 + i];
+      for (const auto& r : region)
+        if (r.first == e.tab) {
+          e.tab = r.second;
+          break;
+        }
+      std::memcpy(&host[base + (size_t)i * (sizeof(DevOp) / 4)], &e, sizeof(DevOp));
+    }
+    for (const auto& r : region) {
+      uint32_t count = 0;
+      for (uint32_t i = 0; i < n; ++i)
+        if (hp.ops[p.op0 + i].tab == r.first) count = hp.ops[p.op0 + i].count;
+      segs.push_back({r.first, (uint32_t)(base + r.second), 2 * count});
+    }
+    pr->img_off[pi] = (uint32_t)base;
+    pr->img_words[pi] = (uint32_t)words;
+  }
+  if (host.empty()) return;
+  cudaStream_t s = pr->ctx->stream;
+  pr->images.alloc(host.size() * 4);
+  QPE_CK(cudaMemcpyAsync(pr->images.p, host.data(), host.size() * 4, cudaMemcpyHostToDevice, s));
+  DevBuf dsegs;
+  dsegs.alloc(segs.size() * sizeof(PassImageSeg));
+  QPE_CK(cudaMemcpyAsync(dsegs.p, segs.data(), segs.size() * sizeof(PassImageSeg), cudaMemcpyHostToDevice, s));
+  QPE_CK(launch_copy_segments(pr->pool.as<uint32_t>(), pr->images.as<uint32_t>(), dsegs.as<PassImageSeg>(),
+                              (uint32_t)segs.size(), s));
+  QPE_CK(cudaStreamSynchronize(s));
+}
+
 static void build_device_program(qpe_program* pr) {
   qpe_context* ctx = pr->ctx;
   HostProgram& hp = pr->hp;
@@ -142,6 +205,7 @@ static void build_device_program(qpe_program* pr) {
                                (uint32_t)hp.tables.size(), total, pr->pool.as<uint32_t>(), s));
   }
   QPE_CK(cudaStreamSynchronize(s));
+  build_pass_images(pr);
 }
 
 // Launch geometry of one pass for elements of esz bytes.
@@ -162,6 +226,12 @@ PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_opt
   PassLaunch pl{};
   pl.err = pr->ctx->err.as<int>();
   pl.bulk = (pass.type != PASS_ROW && (hp.Ca * esz) % 16 == 0) ? 1u : 0u;
+  const size_t pidx = (size_t)(&pass - hp.passes.data());
+  if (pl.bulk && pidx < pr->img_words.size() && pr->img_words[pidx]) {
+    pl.img = pr->images.as<uint32_t>() + pr->img_off[pidx];
+    pl.img_words = pr->img_words[pidx];
+  }
+
   pl.pool = pr->pool.as<uint32_t>();
   pl.ops = pr->ops.as<DevOp>();
   pl.coef = pr->coef.as<double>();
@@ -209,6 +279,10 @@ PassLaunch plan_pass_geometry(const qpe_program* pr, size_t esz, size_t smem_opt
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
   pl.grid = (uint32_t)grid;
+  if (pl.img && pass_smem_bytes(pl, esz) > smem_optin) {  // the image only where it fits beside the stages
+    pl.img = nullptr;
+    pl.img_words = 0;
+  }
   return pl;
 }
 
@@ -532,7 +606,7 @@ static void evolve_tiled(qpe_state* st, const qpe_program* pr, uint32_t first, u
         PassLaunch& pl = plans.back();
         pl.rev = rev ? 1u : 0u;
         pl.exact = exact ? 1u : 0u;
-        size_t sm = pass_stage_elems(pass, pl.Ca, pl.Cb, pl.W) * st->esz * (pl.cta_tile ? 1 : pl.warps_per_cta);
+        const size_t sm = pass_smem_bytes(pl, st->esz);
         if (sm > max_smem) max_smem = sm;
       }
     }

@@ -70,6 +70,10 @@ struct qpe_program {
   uint64_t id = 0;  // unique per process, keys the cached evolution graphs
   qpe::HostProgram hp;
   qpe::DevBuf pool, ops, coef, strA, strB, tabs, start, passes;
+  // MIX pass images (PassLaunch::img): all images back to back, and per pass
+  // its first word and its length in words (0: no image).
+  qpe::DevBuf images;
+  std::vector<uint32_t> img_off, img_words;
 };
 
 namespace qpe {

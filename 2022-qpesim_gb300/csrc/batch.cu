@@ -95,6 +95,10 @@ void plan_class(qpe_batch* b, BatchClass& c) {
       uint32_t wpc = c.wpc ? c.wpc : kCtaTileThreads / 32;
       while (!pl.cta_tile && wpc > 1 && stage * wpc > b->ctx->smem_optin) --wpc;
       pl.warps_per_cta = wpc;
+      if (pl.img && pass_smem_bytes(pl, b->esz) > b->ctx->smem_optin) {  // the image only where it fits
+        pl.img = nullptr;
+        pl.img_words = 0;
+      }
       const uint64_t ntiles = pass.type == PASS_COL ? (hp.Cb + pl.W - 1) / pl.W
                                                     : (pass.type == PASS_ROW ? hp.Ca : pass.mixcount);
       const uint32_t slots = pl.cta_tile ? 1u : wpc;
@@ -114,8 +118,7 @@ void plan_class(qpe_batch* b, BatchClass& c) {
 
 size_t plans_smem(const qpe_batch* b, const BatchClass& c) {
   size_t m = 48 * 1024;
-  for (const PassLaunch& pl : c.plans)
-    m = std::max(m, pass_stage_elems(pl.pass, pl.Ca, pl.Cb, pl.W) * b->esz * (pl.cta_tile ? 1 : pl.warps_per_cta));
+  for (const PassLaunch& pl : c.plans) m = std::max(m, pass_smem_bytes(pl, b->esz));
   return m;
 }
 

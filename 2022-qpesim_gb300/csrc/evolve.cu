@@ -94,6 +94,7 @@ __global__ void k_pass(PassLaunch pl) {
   using C2 = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[CT ? 1 : 32];  // one mbarrier per tile slot (bulk copies)
+  __shared__ __align__(8) uint64_t imgbar;              // the pass image's bulk copy
   const uint32_t lane = CT ? threadIdx.x : (threadIdx.x & 31);  // thread index within the tile
   const uint32_t tpt = CT ? blockDim.x : 32u;                    // threads per tile
   const uint32_t warp = CT ? 0u : (threadIdx.x >> 5);            // tile slot within the CTA
@@ -107,13 +108,24 @@ __global__ void k_pass(PassLaunch pl) {
   const uint32_t* __restrict__ pool = pl.pool;
   const bool bulk = PT != PASS_ROW && pl.bulk != 0;
   const uint32_t bar = static_cast<uint32_t>(__cvta_generic_to_shared(&bars[warp]));
+  // A MIX pass's image (descriptors and tables) in shared memory behind the
+  // stages, brought in once per CTA by one bulk copy.
+  const bool image = PT == PASS_MIX && bulk && pl.img != nullptr;
+  uint32_t* img_s = reinterpret_cast<uint32_t*>(reinterpret_cast<C2*>(smem_raw) + (size_t)wpc * L * W);
+  const uint32_t ibar = static_cast<uint32_t>(__cvta_generic_to_shared(&imgbar));
   if (bulk) {
     if (lane == 0) {
       mbar_init1(bar);
+      if (image && threadIdx.x == 0) mbar_init1(ibar);
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    if (image && threadIdx.x == 0) {
+      mbar_arrive_tx(ibar, pl.img_words * 4u);
+      bulk_load(img_s, pl.img, pl.img_words * 4u, ibar);
+    }
   }
+  bool image_ready = !image;
   uint32_t phase = 0;
   uint32_t ntiles;
   if (PT == PASS_COL) ntiles = (Cb + W - 1) >> logW;
@@ -149,6 +161,7 @@ __global__ void k_pass(PassLaunch pl) {
         }
       }
       bool ok = mbar_wait_bounded(bar, phase);
+      if (!image_ready) ok = mbar_wait_bounded(ibar, 0) && ok;  // the image, before the first tile's terms
       ok = CT ? (__syncthreads_and(ok) != 0) : (__all_sync(0xffffffffu, ok) != 0);  // one verdict per tile
       if (!ok) {
         // the copies did not complete: record it, give the copies in flight one
@@ -156,10 +169,12 @@ __global__ void k_pass(PassLaunch pl) {
         if (lane == 0) {
           atomicOr(pl.err, kPassErrWait);
           mbar_wait_bounded(bar, phase);
+          if (!image_ready) mbar_wait_bounded(ibar, 0);
         }
         break;
       }
       phase ^= 1u;
+      image_ready = true;
     } else {
       // all of the tile's element copies in flight at once (cp.async), so the
       // tile pays the L2 latency once rather than once per element
@@ -172,7 +187,15 @@ __global__ void k_pass(PassLaunch pl) {
       asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
     }
     Sync()();
-    if (PT == PASS_MIX) {
+    if (PT == PASS_MIX && image) {
+      // descriptors and tables from the image: terms 0 .. n - 1 of the pass, the
+      // batch members' coefficients at the pass's own op indices
+      chunked_mix_ops<R, A, false>(reinterpret_cast<const DevOp*>(img_s), pl.coef, img_s, 0u,
+                                   pl.pass.op1 - pl.pass.op0, pl.rev != 0, lane, tpt, true, parb,
+                                   [&](uint32_t a) -> C2& { return st[a]; },
+                                   [&](uint32_t a) -> C2& { return st[Ca + a]; },
+                                   icoef ? icoef + pl.pass.op0 : nullptr, Sync());
+    } else if (PT == PASS_MIX) {
       chunked_mix_ops<R, A>(pl.ops, pl.coef, pool, pl.pass.op0, pl.pass.op1, pl.rev != 0, lane, tpt, true, parb,
                             [&](uint32_t a) -> C2& { return st[a]; }, [&](uint32_t a) -> C2& { return st[Ca + a]; },
                             icoef, Sync());
@@ -220,10 +243,32 @@ size_t pass_stage_elems(const Pass& pass, uint32_t Ca, uint32_t Cb, uint32_t W) 
   return (size_t)Ca * 2;
 }
 
+size_t pass_smem_bytes(const PassLaunch& pl, size_t esz) {
+  return pass_stage_elems(pl.pass, pl.Ca, pl.Cb, pl.W) * esz * (pl.cta_tile ? 1 : pl.warps_per_cta) +
+         (pl.img ? (size_t)pl.img_words * 4 : 0);
+}
+
+// dst[segs[i].dst + k] = src[segs[i].src + k], k < segs[i].words: the tables of
+// the pass images, one CTA per segment.
+__global__ void k_copy_segments(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
+                                const PassImageSeg* __restrict__ segs, uint32_t n) {
+  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+    const PassImageSeg g = segs[i];
+    for (uint32_t k = threadIdx.x; k < g.words; k += blockDim.x) dst[g.dst + k] = src[g.src + k];
+  }
+}
+
+cudaError_t launch_copy_segments(const uint32_t* src, uint32_t* dst, const PassImageSeg* segs, uint32_t n,
+                                 cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_copy_segments<<<n < 4096 ? n : 4096, 128, 0, s>>>(src, dst, segs, n);
+  return cudaGetLastError();
+}
+
 template <typename R, class A, bool CT>
 static cudaError_t launch_ct(const PassLaunch& pl, cudaStream_t s) {
   using C2 = typename Cx<R>::T;
-  const size_t smem = pass_stage_elems(pl.pass, pl.Ca, pl.Cb, pl.W) * sizeof(C2) * (CT ? 1 : pl.warps_per_cta);
+  const size_t smem = pass_smem_bytes(pl, sizeof(C2));
   const dim3 block(CT ? pl.cta_tile : 32 * pl.warps_per_cta);
   switch (pl.pass.type) {
     case PASS_COL: k_pass<R, A, PASS_COL, CT><<<pl.grid, block, smem, s>>>(pl); break;

@@ -61,8 +61,25 @@ struct PassLaunch {
   uint32_t bulk;
   // Device error word: a bounded wait that runs out ORs in kPassErrWait.
   int* err;
+  // A MIX pass's image (with bulk): its term descriptors followed by the tables
+  // they use, the descriptors' table offsets relative to the image, img_words
+  // 32-bit words (a multiple of 4); each CTA brings it into shared memory with
+  // one bulk copy, so the term setup reads at shared-memory latency. nullptr:
+  // descriptors and tables are read from the program in global memory.
+  const uint32_t* img;
+  uint32_t img_words;
 };
 constexpr int kPassErrWait = 2;
+// Largest pass image (bytes) a pass launch stages in shared memory.
+constexpr uint32_t kPassImageMaxBytes = 48 * 1024;
+// Dynamic shared memory of a pass launch: its tile stages and its image.
+size_t pass_smem_bytes(const PassLaunch& pl, size_t esz);
+// One run of words copied from the program's index pool into a pass image.
+struct PassImageSeg {
+  uint32_t src, dst, words;
+};
+cudaError_t launch_copy_segments(const uint32_t* src, uint32_t* dst, const PassImageSeg* segs, uint32_t n,
+                                 cudaStream_t s);
 constexpr uint32_t kCtaTileThreads = 128;
 size_t pass_stage_elems(const Pass& pass, uint32_t Ca, uint32_t Cb, uint32_t W);
 cudaError_t launch_pass(const PassLaunch& pl, int dtype, cudaStream_t s);

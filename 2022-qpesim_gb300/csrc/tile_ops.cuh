@@ -277,7 +277,9 @@ __device__ __forceinline__ void run_mix_ops(const DevOp* __restrict__ ops, const
 // kPairTrips trips cover, runs through run_mix_ops. The update is pair_update's
 // reduced form, bit for bit.
 
-template <typename R, class A, class Left, class Right, class Sync>
+// G: descriptors and tables in global memory (read through the read-only
+// cache); false when the caller has staged them in shared memory (a pass image).
+template <typename R, class A, bool G = true, class Left, class Right, class Sync>
 __device__ __forceinline__ void chunked_mix_ops(const DevOp* __restrict__ ops, const double* __restrict__ coef,
                                                 const uint32_t* __restrict__ pool, uint32_t op0, uint32_t op1,
                                                 bool rev, uint32_t jl, uint32_t jstep, bool active, uint32_t parb,
@@ -287,8 +289,8 @@ __device__ __forceinline__ void chunked_mix_ops(const DevOp* __restrict__ ops, c
   // The terms of a MIX pass share one table length (pairs of alpha strings for
   // one excitation): passes whose tables need more trips skip the chunked form.
   if (n == 0) return;
-  if (__ldg(reinterpret_cast<const uint4*>(ops + op0)).y > kPairTrips * jstep) {
-    run_mix_ops<R, A, true>(ops, coef, pool, op0, op1, rev, jl, jstep, active, parb, left, right, icoef, sync);
+  if (ldm<G>(reinterpret_cast<const uint4*>(ops + op0)).y > kPairTrips * jstep) {
+    run_mix_ops<R, A, G>(ops, coef, pool, op0, op1, rev, jl, jstep, active, parb, left, right, icoef, sync);
     return;
   }
   for (uint32_t i0 = 0; i0 < n; i0 += kPairChunk) {
@@ -308,7 +310,7 @@ __device__ __forceinline__ void chunked_mix_ops(const DevOp* __restrict__ ops, c
       if (k < m) {
         const uint32_t o = rev ? op1 - 1 - (i0 + k) : op0 + i0 + k;
         const uint4* src = reinterpret_cast<const uint4*>(ops + o);
-        const uint4 a = __ldg(src), b = __ldg(src + 1);
+        const uint4 a = ldm<G>(src), b = ldm<G>(src + 1);
         fast = fast && a.w == OP_INLINE && (a.z & 0xffu) == (uint32_t)OPK_PAIR && a.y <= kPairTrips * jstep;
         double c0 = __hiloint2double((int)b.y, (int)b.x), c1 = __hiloint2double((int)b.w, (int)b.z);
         if (icoef) {
@@ -322,7 +324,7 @@ __device__ __forceinline__ void chunked_mix_ops(const DevOp* __restrict__ ops, c
         for (uint32_t tr = 0; tr < kPairTrips; ++tr) {
           const uint32_t j = jl + tr * jstep;
           if (active && j < a.y) {
-            const uint2 x = __ldg(reinterpret_cast<const uint2*>(pool + a.x) + j);
+            const uint2 x = ldm<G>(reinterpret_cast<const uint2*>(pool + a.x) + j);
             lp[k][tr] = &left(x.x & 0x7fffffffu);
             rp[k][tr] = &right(x.y);
             par[k] |= (((x.x >> 31) ^ parb) & 1u) << tr;
@@ -332,7 +334,7 @@ __device__ __forceinline__ void chunked_mix_ops(const DevOp* __restrict__ ops, c
       }
     }
     if (!fast) {
-      run_mix_ops<R, A, true>(ops, coef, pool, rev ? op1 - (i0 + m) : op0 + i0, rev ? op1 - i0 : op0 + i0 + m, rev,
+      run_mix_ops<R, A, G>(ops, coef, pool, rev ? op1 - (i0 + m) : op0 + i0, rev ? op1 - i0 : op0 + i0 + m, rev,
                               jl, jstep, active, parb, left, right, icoef, sync);
       continue;
     }
