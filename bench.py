@@ -146,7 +146,11 @@ def measure_fp64_peak(N, ctx):
     return v.value
 
 
-def roofline_single(w, achieved, peak, peak_kind, kernel, touches_step, ev_s, fp64_peak):
+GB300_SMS = 152  # the SMs of one GB300 (the only target)
+
+
+def roofline_single(w, achieved, peak, peak_kind, kernel, touches_step, ev_s, fp64_peak, cluster_sms=0,
+                    num_sms=GB300_SMS):
     """Roofline object of a single-instance workload. achieved is the algorithmic
     HBM figure (2 * sizeof(amplitude) per touch over the evolution time); `bound`
     names the resource that limits the dominant kernel, as measured."""
@@ -163,6 +167,9 @@ def roofline_single(w, achieved, peak, peak_kind, kernel, touches_step, ev_s, fp
         r["fp64"] = {"achieved_tflops": ops, "peak_fma_tflops": fp64_peak,
                      "frac_of_fma_peak": ops / fp64_peak if fp64_peak else None,
                      "frac_of_issue_rate": 2 * ops / fp64_peak if fp64_peak else None,
+                     "frac_of_cluster_issue_rate": (2 * ops / (fp64_peak * cluster_sms / num_sms)
+                                                    if fp64_peak and cluster_sms else None),
+                     "cluster_sms": cluster_sms,
                      "ops_per_touch": 6,
                      "peak_method": "measured live in this run by qpe_measure_fp64_peak (an FMA counts 2 FLOP; "
                                     "the path issues DMUL and DADD, so its ceiling is half the FMA FLOP/s: "
@@ -428,7 +435,8 @@ def run_ours(args, w, rank, ws, local):
         "data": DATA_NOTE,
         "config": workload_config(args, w, prog.touches_per_power, ws),
         "kernel_strategy": strategy_name,
-        "roofline": roofline_single(w, achieved, peak, peak_kind, kernel, touches_step, ev_s, fp64_peak),
+        "roofline": roofline_single(w, achieved, peak, peak_kind, kernel, touches_step, ev_s, fp64_peak,
+                                    cluster_sms=kc if strat in (2, 4, 5, 6) else (1 if strat == 1 else 0)),
         "e2e": {"value": e2e_value, "unit": "touches/s",
                 "h2d_bytes_per_step": int(st.ld * dtype().itemsize),
                 "d2h_bytes_per_step": int(st.size * dtype().itemsize + (1 << P) * 8)},
