@@ -49,6 +49,8 @@ struct GemmArgs {
   int* err;              // set when a wait runs out
   uint32_t ksplit;       // EPI_F32: CTAs along K (grid z); slice z writes out + z * split_stride
   size_t split_stride;
+  bf16* out_t;           // BF16 epilogues: if set, the output transposed as well ([N, M], row stride ldt),
+  uint32_t ldt;          //   the K-major operand of the weight-gradient product (no separate transpose)
 };
 
 constexpr uint32_t kStages = 4;
@@ -193,6 +195,12 @@ __global__ void __launch_bounds__(128, 1)
       uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<bf16*>(g.out) + off);
       o[0] = reinterpret_cast<const uint4*>(h)[0];
       o[1] = reinterpret_cast<const uint4*>(h)[1];
+      if (g.out_t) {
+        // a warp's 32 lanes hold 32 consecutive rows: each transposed column is
+        // one 64-byte run
+#pragma unroll
+        for (int i = 0; i < 16; ++i) g.out_t[(size_t)(col + i) * g.ldt + row] = h[i];
+      }
     }
   }
   umma::fence_before_sync();
@@ -298,46 +306,80 @@ __global__ void k_loss(const float* __restrict__ Y, const float* __restrict__ bl
   if (threadIdx.x == 0) atomicAdd(loss, red[0]);
 }
 
-// Column sums of a BF16 matrix in two fixed-order phases: block b sums rows
-// [256 b, 256 b + 256) of every column into part[b, c]; then part's rows are
-// summed in order into out[c].
-constexpr uint32_t kColsumRows = 256;
+constexpr uint32_t kColsumRows = 64;
+
+// Column sums of a [R x C] BF16 matrix (row stride lds, C and lds even) in two
+// fixed-order phases: k_colsum_part writes one partial row per kColsumRows rows
+// (each thread two columns, four independent accumulators over rows r = j mod 4),
+// k_colsum_final adds the partial rows of a column in a fixed tree.
 __global__ void k_colsum_part(const bf16* __restrict__ src, uint32_t R, uint32_t C, uint32_t lds,
                               float* __restrict__ part) {
-  const uint32_t c = threadIdx.x, r0 = blockIdx.x * kColsumRows;
+  const uint32_t c = 2 * threadIdx.x, r0 = blockIdx.x * kColsumRows;
   if (c >= C) return;
-  float s = 0.f;
   const uint32_t r1 = min(R, r0 + kColsumRows);
-#pragma unroll 8
-  for (uint32_t r = r0; r < r1; ++r) s += __bfloat162float(src[(size_t)r * lds + c]);
-  part[(size_t)blockIdx.x * C + c] = s;
+  float2 a[4] = {};
+  for (uint32_t r = r0; r < r1; r += 4) {
+#pragma unroll
+    for (uint32_t j = 0; j < 4; ++j) {
+      if (r + j < r1) {
+        const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(src + (size_t)(r + j) * lds + c));
+        a[j].x += v.x;
+        a[j].y += v.y;
+      }
+    }
+  }
+  part[(size_t)blockIdx.x * C + c] = (a[0].x + a[1].x) + (a[2].x + a[3].x);
+  part[(size_t)blockIdx.x * C + c + 1] = (a[0].y + a[1].y) + (a[2].y + a[3].y);
 }
 __global__ void k_colsum_final(const float* __restrict__ part, uint32_t nparts, uint32_t C, float* __restrict__ out) {
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= C) return;
+  __shared__ float red[4];
+  const uint32_t c = blockIdx.x;  // one CTA of 128 threads per column
   float s = 0.f;
-  for (uint32_t p = 0; p < nparts; ++p) s += part[(size_t)p * C + c];
-  out[c] = s;
+  for (uint32_t p = threadIdx.x; p < nparts; p += blockDim.x) s += part[(size_t)p * C + c];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) out[c] = (red[0] + red[1]) + (red[2] + red[3]);
 }
 
-// Adam on one parameter block; writes the BF16 copy (rows x cols, stride ldb)
-// and, if given, its transpose (cols x rows, stride ldt).
+// One parameter block of the Adam step: its offset in the parameter, moment and
+// gradient arrays (the gradient block has the same layout), its shape, and the
+// BF16 copy (rows x cols, stride ldb) and transpose (cols x rows, stride ldt)
+// it refreshes (null: none).
+struct AdamBlock {
+  uint32_t off, rows, cols, ldb, ldt;
+  bf16* wb;
+  bf16* wt;
+};
+constexpr int kAdamBlocks = 8;
+struct AdamBlocks {
+  AdamBlock b[kAdamBlocks];
+  uint32_t start[kAdamBlocks + 1];  // flattened element index of each block's first element
+};
+
+// Adam over every parameter block in one launch: thread i updates flattened
+// element i, finds its block from `start`, and writes the block's BF16 copy and
+// transpose.
 __global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                       const float* __restrict__ grad, uint32_t rows, uint32_t cols, uint32_t ldg, float lr, float b1,
-                       float b2, float eps, float c1, float c2, bf16* __restrict__ wb, uint32_t ldb,
-                       bf16* __restrict__ wt, uint32_t ldt) {
+                       const float* __restrict__ grad, const __grid_constant__ AdamBlocks blocks, float lr, float b1,
+                       float b2, float eps, float c1, float c2) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= rows * cols) return;
-  const uint32_t r = i / cols, c = i - r * cols;
-  const float gr = grad[(size_t)r * ldg + c];
-  const float mi = b1 * m[i] + (1.f - b1) * gr;
-  const float vi = b2 * v[i] + (1.f - b2) * gr * gr;
-  m[i] = mi;
-  v[i] = vi;
-  const float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
-  w[i] = wi;
-  if (wb) wb[(size_t)r * ldb + c] = __float2bfloat16_rn(wi);
-  if (wt) wt[(size_t)c * ldt + r] = __float2bfloat16_rn(wi);
+  if (i >= blocks.start[kAdamBlocks]) return;
+  int k = 0;
+#pragma unroll
+  for (int q = 1; q < kAdamBlocks; ++q) k += i >= blocks.start[q] ? 1 : 0;
+  const AdamBlock& B = blocks.b[k];
+  const uint32_t e = i - blocks.start[k], r = e / B.cols, c = e - r * B.cols;
+  const size_t o = (size_t)B.off + e;
+  const float gr = grad[o];
+  const float mi = b1 * m[o] + (1.f - b1) * gr;
+  const float vi = b2 * v[o] + (1.f - b2) * gr * gr;
+  m[o] = mi;
+  v[o] = vi;
+  const float wi = w[o] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  w[o] = wi;
+  if (B.wb) B.wb[(size_t)r * B.ldb + c] = __float2bfloat16_rn(wi);
+  if (B.wt) B.wt[(size_t)c * B.ldt + r] = __float2bfloat16_rn(wi);
 }
 
 __global__ void k_cast_bf16(const float* __restrict__ w, uint32_t rows, uint32_t cols, bf16* __restrict__ wb,
@@ -434,7 +476,7 @@ static Gemm make_gemm(int epi, uint32_t bn, const void* A, uint32_t lda, const v
   Gemm G;
   G.ta = make_map(A, M, K, lda, 128);
   G.tb = make_map(B, N, K, ldb, bn);
-  G.g = GemmArgs{M, N, K, bias, out, ldo, pre_out, pre_in, err, 1u, 0};
+  G.g = GemmArgs{M, N, K, bias, out, ldo, pre_out, pre_in, err, 1u, 0, nullptr, 0};
   G.epi = epi;
   G.bn = bn;
   return G;
@@ -520,7 +562,7 @@ static void mlp_alloc(qpe_mlp* m) {
   m->X0T.alloc(K0 * Bp * b2);
   for (DevBuf* p : {&m->H1T, &m->H2T, &m->H3T, &m->dZ1T, &m->dZ2T, &m->dZ3T}) p->alloc(H * Bp * b2);
   m->dYT.alloc(128 * Bp * b2);  // 128 rows for the M = 128 tile; rows past 63 stay zero
-  m->colpart.alloc(((Bp + 255) / 256) * H * 4);
+  m->colpart.alloc(((Bp + kColsumRows - 1) / kColsumRows) * H * 4);
   const size_t splitk_elems = (size_t)64 * 256 * 256;  // up to 64 K slices of a 256 x 256 gradient
   m->splitk.alloc(splitk_elems * 4);
   m->bla.alloc(Bp * 4);
@@ -552,6 +594,15 @@ static void mlp_alloc(qpe_mlp* m) {
                 m->pre2.as<float>(), err),
       make_gemm(EPI_DGELU, 256, m->dZ2.p, 256, m->W2t.p, 256, B, 256, 256, m->dZ1.p, 256, nullptr, nullptr,
                 m->pre1.as<float>(), err)};
+  // the BF16 epilogues also write the transposed activations the weight-gradient
+  // products read (H1..H3 and dZ1..dZ3, [256, B])
+  m->fwd[0].g.out_t = m->H1T.as<bf16>();
+  m->fwd[1].g.out_t = m->H2T.as<bf16>();
+  m->fwd[2].g.out_t = m->H3T.as<bf16>();
+  m->bwd[0].g.out_t = m->dZ3T.as<bf16>();
+  m->bwd[1].g.out_t = m->dZ2T.as<bf16>();
+  m->bwd[2].g.out_t = m->dZ1T.as<bf16>();
+  for (Gemm* g : {&m->fwd[0], &m->fwd[1], &m->fwd[2], &m->bwd[0], &m->bwd[1], &m->bwd[2]}) g->g.ldt = B;
   // dW4 is [128, 256] over the padded dY^T, stored past the parameter blocks;
   // its rows 0..15 are copied into the W4 block.
   const uint32_t sms = (uint32_t)m->ctx->num_sms;
@@ -599,22 +650,17 @@ static void backward(qpe_mlp* m, uint32_t count, cudaStream_t s, float* loss) {
   auto tr = [&](const DevBuf& src, uint32_t R, uint32_t C, uint32_t lds, DevBuf& dst, uint32_t ldd) {
     k_transpose<<<dim3((C + 31) / 32, (R + 31) / 32), tb, 0, s>>>(src.as<bf16>(), dst.as<bf16>(), R, C, lds, ldd);
   };
+  // H1..H3 and dZ1..dZ3 were written transposed by their GEMMs' epilogues
   tr(m->X0, B, 64, 64, m->X0T, B);
-  tr(m->H1, B, 256, 256, m->H1T, B);
-  tr(m->H2, B, 256, 256, m->H2T, B);
-  tr(m->H3, B, 256, 256, m->H3T, B);
   tr(m->dY, B, 64, 64, m->dYT, B);
-  tr(m->dZ1, B, 256, 256, m->dZ1T, B);
-  tr(m->dZ2, B, 256, 256, m->dZ2T, B);
-  tr(m->dZ3, B, 256, 256, m->dZ3T, B);
   QPE_CK(cudaGetLastError());
   for (const Gemm& g : m->wgrad) QPE_CK(launch_gemm(g, s));
   float* G = m->grads.as<float>();
   QPE_CK(cudaMemcpyAsync(G + qpe_mlp::oW4, G + qpe_mlp::nparams, 16 * 256 * 4, cudaMemcpyDeviceToDevice, s));
   const uint32_t nparts = (B + kColsumRows - 1) / kColsumRows;
   auto colsum = [&](const DevBuf& src, uint32_t C, uint32_t lds, float* out) {
-    k_colsum_part<<<nparts, 256, 0, s>>>(src.as<bf16>(), B, C, lds, m->colpart.as<float>());
-    k_colsum_final<<<1, 256, 0, s>>>(m->colpart.as<float>(), nparts, C, out);
+    k_colsum_part<<<nparts, 128, 0, s>>>(src.as<bf16>(), B, C, lds, m->colpart.as<float>());
+    k_colsum_final<<<C, 128, 0, s>>>(m->colpart.as<float>(), nparts, C, out);
   };
   colsum(m->dZ1, 256, 256, G + qpe_mlp::ob1);
   colsum(m->dZ2, 256, 256, G + qpe_mlp::ob2);
@@ -628,19 +674,25 @@ static void adam(qpe_mlp* m, float lr, cudaStream_t s, float c1, float c2) {
   float* M1 = m->mom1.as<float>();
   float* M2 = m->mom2.as<float>();
   float* G = m->grads.as<float>();
-  auto step = [&](size_t off, uint32_t rows, uint32_t cols, void* wb, uint32_t ldb, void* wt, uint32_t ldt) {
-    k_adam<<<(rows * cols + 255) / 256, 256, 0, s>>>(P + off, M1 + off, M2 + off, G + off, rows, cols, cols, lr, 0.9f,
-                                                     0.999f, 1e-8f, c1, c2, (bf16*)wb, ldb, (bf16*)wt, ldt);
-  };
-  step(qpe_mlp::oW1, 256, 64, m->W1b.p, 64, nullptr, 0);
-  step(qpe_mlp::ob1, 1, 256, nullptr, 0, nullptr, 0);
-  step(qpe_mlp::oW2, 256, 256, m->W2b.p, 256, m->W2t.p, 256);
-  step(qpe_mlp::ob2, 1, 256, nullptr, 0, nullptr, 0);
-  step(qpe_mlp::oW3, 256, 256, m->W3b.p, 256, m->W3t.p, 256);
-  step(qpe_mlp::ob3, 1, 256, nullptr, 0, nullptr, 0);
   // only the two live outputs of the last layer train; the padding stays zero
-  step(qpe_mlp::oW4, 2, 256, m->W4b.p, 256, m->W4t.p, 64);
-  step(qpe_mlp::ob4, 1, 2, nullptr, 0, nullptr, 0);
+  const AdamBlock list[kAdamBlocks] = {
+      {qpe_mlp::oW1, 256, 64, 64, 0, (bf16*)m->W1b.p, nullptr},
+      {qpe_mlp::ob1, 1, 256, 0, 0, nullptr, nullptr},
+      {qpe_mlp::oW2, 256, 256, 256, 256, (bf16*)m->W2b.p, (bf16*)m->W2t.p},
+      {qpe_mlp::ob2, 1, 256, 0, 0, nullptr, nullptr},
+      {qpe_mlp::oW3, 256, 256, 256, 256, (bf16*)m->W3b.p, (bf16*)m->W3t.p},
+      {qpe_mlp::ob3, 1, 256, 0, 0, nullptr, nullptr},
+      {qpe_mlp::oW4, 2, 256, 256, 64, (bf16*)m->W4b.p, (bf16*)m->W4t.p},
+      {qpe_mlp::ob4, 1, 2, 0, 0, nullptr, nullptr}};
+  AdamBlocks ab{};
+  uint32_t total = 0;
+  for (int k = 0; k < kAdamBlocks; ++k) {
+    ab.b[k] = list[k];
+    ab.start[k] = total;
+    total += list[k].rows * list[k].cols;
+  }
+  ab.start[kAdamBlocks] = total;
+  k_adam<<<(total + 255) / 256, 256, 0, s>>>(P, M1, M2, G, ab, lr, 0.9f, 0.999f, 1e-8f, c1, c2);
   QPE_CK(cudaGetLastError());
 }
 
