@@ -99,10 +99,11 @@ MEASURED_TRAFFIC = {
     "plain-n16": (338_944, "k_resident_lean, cluster of 16: one launch runs every power; the capture of a "
                            "2-power launch read the block and the program once (0.34 MB) and wrote nothing back to "
                            "DRAM, the snapshots staying in L2 (ncu capture of the same kernel, small case)"),
-    "precision-n24": (6_876_160, "k_pass MIX launch, one tile per CTA: the 6.9 MB working block read once, cold "
-                                 "cache under ncu (capture at P = 3; the working block is the same at any P)"),
-    "batched-256": (28_700_000, "k_pass MIX launch: 3.59 MB for the 32-instance draw, scaled by the 8x members "
-                                "per launch"),
+    "precision-n24": (3_810_000, "k_pass MIX launch, one tile per CTA, pass image in shared memory: DRAM reads "
+                                 "of a cold-cache ncu capture at P = 3 (3.79-3.82 MB; the 6.8 MB working block is "
+                                 "the same at any P, and a MIX pass touches its column pairs, about half of it)"),
+    "batched-256": (16_650_000, "k_pass MIX launch: 2.08 MB for the 32-instance draw (cold-cache ncu capture), "
+                                "scaled by the 8x members per launch"),
 }
 
 
