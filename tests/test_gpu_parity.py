@@ -477,3 +477,37 @@ def test_fp64_peak_probe(gpu):
     v = ctypes.c_double()
     N.check(N.lib().qpe_measure_fp64_peak(N.context(0), ctypes.byref(v)))
     assert 0.1 < v.value < 200.0, v.value
+
+
+@pytest.mark.parametrize("n,na,nb,order", [(14, 4, 3, 1), (14, 3, 4, 2), (10, 2, 2, 1), (16, 4, 4, 2)])
+def test_tile_passes_complex64_copy_paths(gpu, orc, n, na, nb, order):
+    """complex64 tile passes on both copy paths: columns of 8 x Ca bytes that are
+    not a multiple of 16 (Ca = 35 at n = 14, Na = 4; Ca = 35 with the spins
+    swapped in the second case) take per-thread copies, the others bulk copies
+    and the pass images; all within 2e-5 of the complex128 oracle, and the
+    complex128 tile passes on the same shapes bit for bit."""
+    q = gpu
+    M, P = n // 2, 3
+    seg = _seg(q, n, 2 * max(na, nb), 700 + n + na, 0.06)
+    prog = q.Program(seg, M, na, nb, trotter_order=order, steps=2 if order == 2 else 1)
+    steps = 2 if order == 2 else 1
+    ref = None
+    for dtype in (np.complex64, np.complex128):
+        st = q.DeviceState(M, na, nb, P, dtype=dtype)
+        b0 = q.hf_block0(st.c_alpha, st.c_beta, P)
+        rng = np.random.default_rng(n + na)
+        b0 = b0 + (rng.standard_normal(st.ld) + 1j * rng.standard_normal(st.ld)) * 1e-2
+        st.upload(b0.astype(dtype))
+        st.evolve(prog, strategy=3)
+        if ref is None:
+            ref = np.zeros(st.size, np.complex128)
+            ref[:st.ld] = b0.astype(np.complex64)
+            orc.time_evolve(M, na, nb, P, seg, ref, order=order, steps=steps)
+        got = st.download()
+        if dtype == np.complex64:
+            assert np.abs(got - ref).max() < 2e-5
+        else:
+            ref128 = np.zeros(st.size, np.complex128)
+            ref128[:st.ld] = b0
+            orc.time_evolve(M, na, nb, P, seg, ref128, order=order, steps=steps)
+            assert np.array_equal(got, ref128)
