@@ -14,7 +14,7 @@ import math
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden_segments, load_golden, reference_root
+from conftest import golden_segments, load_golden, reference_root
 from test_term_compiler import _assert_segments
 
 _REF_ROOT = reference_root()
