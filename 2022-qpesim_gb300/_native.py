@@ -92,6 +92,7 @@ PROTOTYPES = {
     "qpe_program_plan": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32] + [_P_TERM, C.c_size_t] * 5
                          + [C.c_uint32, C.c_uint32, C.POINTER(ProgramInfo)]),
     "qpe_program_get_info": (C.c_int, [_vp, C.POINTER(ProgramInfo)]),
+    "qpe_program_unit_schedule": (C.c_int, [_vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "qpe_state_create": (C.c_int, [_vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.POINTER(_vp)]),
     "qpe_state_destroy": (C.c_int, [_vp]),
     "qpe_state_upload": (C.c_int, [_vp, _vp, C.c_uint64, C.c_uint64]),

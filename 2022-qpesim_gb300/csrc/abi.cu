@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "abi_internal.h"
+#include "mix_units.h"
 
 namespace qpe {
 
@@ -315,9 +316,11 @@ static uint32_t choose_lines(uint64_t lines, uint64_t nwarps, uint64_t entries) 
 
 // Geometry of k_resident_lean for cluster size K: three-warp groups (15, 12, 9,
 // 6 or 3 warps per CTA), one line or column pair per group tile, a stage of one
-// column pair (2 Ca elements) per group when K > 1.
+// column pair (2 Ca elements) per group when K > 1. With `units` (K > 1) every
+// warp also gets a shared-memory slot for its warp program of the column-pair
+// update units (mix_units.h).
 static bool plan_resident_lean(const qpe_program* pr, const qpe_state* st, uint32_t K, ResidentLaunch& rl,
-                               ResidentInstance& ri) {
+                               ResidentInstance& ri, bool units = false) {
   const HostProgram& hp = pr->hp;
   const size_t esz = st->esz;
   const uint64_t Ca = hp.Ca, Cb = hp.Cb;
@@ -325,11 +328,15 @@ static bool plan_resident_lean(const qpe_program* pr, const qpe_state* st, uint3
   const size_t meta = resident_meta_bytes((uint32_t)hp.ops.size(), (uint32_t)hp.pool_words,
                                           (uint32_t)hp.passes.size(), (uint32_t)Ca, (uint32_t)Cb);
   const uint64_t stage = K > 1 ? 2 * Ca : 0;
+  if (units && K < 2) return false;
+  const size_t wp_bytes = units ? (size_t)mix_wp_words(hp) * 4 : 0;
   for (int with_meta = 1; with_meta >= 0; --with_meta)
     for (uint32_t wpc = 15; wpc >= 3; wpc -= 3) {
-      // block rows, group stages, the row-pointer table (Ca generic pointers), then the metadata
+      // block rows, group stages, the row-pointer table (Ca generic pointers), the
+      // warp-program slots, then the metadata
       const size_t head = (size_t)(Rk * Cb * esz + (wpc / 3) * stage * esz);
-      const size_t rows = ((head + 15) & ~(size_t)15) + ((Ca * sizeof(void*) + 15) & ~(size_t)15);
+      const size_t rows =
+          ((head + 15) & ~(size_t)15) + ((Ca * sizeof(void*) + 15) & ~(size_t)15) + wpc * wp_bytes;
       const size_t smem = with_meta ? rows + meta : rows;
       if (smem + kResidentStaticSmem > st->ctx->smem_optin) continue;
       ri = ResidentInstance{};
@@ -357,7 +364,7 @@ static bool plan_resident_lean(const qpe_program* pr, const qpe_state* st, uint3
 // single warps, one stage per warp (a group uses its four warps' stages).
 static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K, ResidentLaunch& rl,
                           ResidentInstance& ri, uint32_t mode = 0) {
-  if (mode == 3) return plan_resident_lean(pr, st, K, rl, ri);
+  if (mode == 3 || mode == 4) return plan_resident_lean(pr, st, K, rl, ri, mode == 4);
   const bool group = mode == 1;
   const HostProgram& hp = pr->hp;
   const size_t esz = st->esz;
@@ -412,12 +419,50 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
   return false;
 }
 
+// Most consecutive column-pair passes one window of update units may take.
+constexpr uint32_t kMixWindowPasses = 4;
+
+// The column-pair update-unit schedule of `pr` for cluster K, wpc warps per CTA
+// and group stages of `stage` elements, built from the device's index pool on
+// first use and kept with the program. False if no pass could be scheduled.
+static bool ensure_mix_units(const qpe_program* pr, uint32_t K, uint32_t wpc, uint32_t stage) {
+  if (pr->mix_wp_words && pr->mix_K == K && pr->mix_wpc == wpc && pr->mix_stage == stage)
+    return pr->mix_scheduled > 0;
+  const HostProgram& hp = pr->hp;
+  cudaStream_t s = pr->ctx->stream;
+  std::vector<uint32_t> pool(hp.pool_words);
+  QPE_CK(cudaMemcpyAsync(pool.data(), pr->pool.p, pool.size() * 4, cudaMemcpyDeviceToHost, s));
+  QPE_CK(cudaStreamSynchronize(s));
+  MixUnits mu;
+  build_mix_units(hp, pool.data(), K, wpc, stage, kMixWindowPasses, mu);
+  pr->mix_words.release();
+  pr->mix_slot.release();
+  if (mu.scheduled) {
+    pr->mix_words.alloc(mu.words.size() * 4);
+    pr->mix_slot.alloc(mu.pass_slot.size() * 4);
+    QPE_CK(cudaMemcpyAsync(pr->mix_words.p, mu.words.data(), mu.words.size() * 4, cudaMemcpyHostToDevice, s));
+    QPE_CK(cudaMemcpyAsync(pr->mix_slot.p, mu.pass_slot.data(), mu.pass_slot.size() * 4, cudaMemcpyHostToDevice, s));
+    QPE_CK(cudaStreamSynchronize(s));
+  }
+  pr->mix_K = K;
+  pr->mix_wpc = wpc;
+  pr->mix_stage = stage;
+  pr->mix_wp_words = mu.wp_words ? mu.wp_words : mix_wp_words(hp);
+  pr->mix_scheduled = mu.scheduled;
+  return mu.scheduled > 0;
+}
+
 static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint32_t first, uint32_t last,
                          bool exact, bool in_place = false, uint32_t mode = 0) {
   ResidentLaunch rl;
   ResidentInstance ri{};
   if (!plan_resident(pr, st, K, rl, ri, mode))
     throw Error(QPE_ERR_UNSUPPORTED, "block does not fit the cluster's shared memory");
+  if (mode == 4 && ensure_mix_units(pr, K, rl.warps_per_cta, rl.stage_elems)) {
+    ri.mix_words = pr->mix_words.as<uint32_t>();
+    ri.mix_slot = pr->mix_slot.as<uint32_t>();
+    ri.mix_wp_words = pr->mix_wp_words;
+  }
   ri.state = st->data.p;
   ri.pool = pr->pool.as<uint32_t>();
   ri.ops = pr->ops.as<DevOp>();
@@ -451,6 +496,7 @@ static uint32_t resident_mode(uint32_t strategy) {
   if (strategy == QPE_STRATEGY_GROUP) return 1u;
   if (strategy == QPE_STRATEGY_HYBRID) return 2u;
   if (strategy == QPE_STRATEGY_LEAN) return 3u;
+  if (strategy == QPE_STRATEGY_LEAN_UNITS) return 4u;
   return 0u;
 }
 
@@ -466,7 +512,7 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     return;
   }
   if (strategy == QPE_STRATEGY_CLUSTER || strategy == QPE_STRATEGY_GROUP || strategy == QPE_STRATEGY_HYBRID ||
-      strategy == QPE_STRATEGY_LEAN) {
+      strategy == QPE_STRATEGY_LEAN || strategy == QPE_STRATEGY_LEAN_UNITS) {
     const uint32_t mode = resident_mode(strategy);
     if (K == 0) {
       for (uint32_t c = mode ? 1 : 2; c <= 16 && !K; c *= 2)
@@ -498,6 +544,8 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     if (plan_resident(pr, st, c, rl, ri, 1)) cands.push_back({QPE_STRATEGY_GROUP, c});
     if (plan_resident(pr, st, c, rl, ri, 2)) cands.push_back({QPE_STRATEGY_HYBRID, c});
     if (plan_resident(pr, st, c, rl, ri, 3)) cands.push_back({QPE_STRATEGY_LEAN, c});
+    if (plan_resident(pr, st, c, rl, ri, 4) && ensure_mix_units(pr, c, rl.warps_per_cta, rl.stage_elems))
+      cands.push_back({QPE_STRATEGY_LEAN_UNITS, c});
   }
   cands.push_back({QPE_STRATEGY_TILED, 0});
   if (cands.size() == 1) {
@@ -978,6 +1026,13 @@ int qpe_program_get_info(const qpe_program* pr, qpe_program_info* info) {
   return QPE_OK;
 }
 
+int qpe_program_unit_schedule(const qpe_program* pr, uint32_t* cluster_size, uint32_t* scheduled_passes) {
+  if (!pr || !cluster_size || !scheduled_passes) return fail(QPE_ERR_INVALID, "null argument");
+  *cluster_size = pr->mix_wp_words ? pr->mix_K : 0u;
+  *scheduled_passes = pr->mix_wp_words ? pr->mix_scheduled : 0u;
+  return QPE_OK;
+}
+
 static void fill_info(const HostProgram& hp, qpe_program_info* info) {
   info->num_orbitals = hp.M;
   info->n_alpha = hp.na;
@@ -1071,7 +1126,7 @@ int qpe_evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts
   return guard([&] {
     check_state(st);
     if (!pr) throw Error(QPE_ERR_INVALID, "null program");
-    if (opts && opts->strategy > QPE_STRATEGY_LEAN) throw Error(QPE_ERR_INVALID, "unknown strategy");
+    if (opts && opts->strategy > QPE_STRATEGY_LEAN_UNITS) throw Error(QPE_ERR_INVALID, "unknown strategy");
     if (opts && opts->cluster_size && (opts->cluster_size > 16 || (opts->cluster_size & (opts->cluster_size - 1))))
       throw Error(QPE_ERR_INVALID, "cluster_size must be a power of two <= 16");
     if (opts && (opts->flags & ~(QPE_EVOLVE_FP64_CONTRACT | QPE_EVOLVE_IN_PLACE)))

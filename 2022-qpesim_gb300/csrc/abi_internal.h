@@ -74,6 +74,11 @@ struct qpe_program {
   // its first word and its length in words (0: no image).
   qpe::DevBuf images;
   std::vector<uint32_t> img_off, img_words;
+  // Update-unit schedule of the column-pair passes (mix_units.h) for the lean
+  // resident kernel, built on first use for one geometry (cluster, warps per
+  // CTA, stage) and kept: mix_slot per pass, mix_words the warp programs.
+  mutable qpe::DevBuf mix_words, mix_slot;
+  mutable uint32_t mix_K = 0, mix_wpc = 0, mix_stage = 0, mix_wp_words = 0, mix_scheduled = 0;
 };
 
 namespace qpe {

@@ -119,6 +119,12 @@ struct ResidentInstance {
   uint32_t nops, pool_words;  // sizes of the term descriptors and the index pool
   uint32_t in_place;        // 1: block `first` is loaded, evolved last - first times
                             //    and written back to itself (iterative QPE)
+  // Column-pair passes as update units (mix_units.h; k_resident_lean only): the
+  // warp programs, per pass its block of them or kMixNoSchedule, and the words
+  // of one program. mix_words == nullptr: every column-pair pass by tiles.
+  const uint32_t* mix_words;
+  const uint32_t* mix_slot;
+  uint32_t mix_wp_words;
 };
 struct ResidentLaunch {
   const ResidentInstance* insts;  // device array, ninst entries

@@ -1,0 +1,293 @@
+// mix_units.cpp - the host scheduler of the column-pair passes' update units
+// (mix_units.h).
+#include "mix_units.h"
+
+#include <algorithm>
+#include <numeric>
+
+namespace qpe {
+
+namespace {
+
+constexpr uint32_t kQuads = 8;         // quads of lanes per warp
+constexpr uint32_t kLanes = 32;        // amplitudes a warp gathers (one per lane)
+constexpr uint32_t kMaxTeam = 3;       // warps of a three-warp group
+constexpr uint32_t kIdxLimit = 1024;   // stage indices are 10-bit
+constexpr uint32_t kLineLimit = 2048;  // rows and columns are 11-bit
+
+struct Upd {
+  uint32_t l, r, par;  // unit-local amplitude indices, parity of the update
+};
+
+// One connected component of a window's pairings: its amplitudes (row * Cb +
+// col) and its updates per level.
+struct Comp {
+  std::vector<uint32_t> nodes;
+  std::vector<std::vector<Upd>> lev;
+  uint32_t maxper = 0;
+};
+
+// Work placed on warps: one unit on a team of `tw` warps, or several small units
+// on one warp (tw = 1).
+struct Team {
+  uint32_t tw = 1;
+  std::vector<uint32_t> units;
+  uint32_t quads = 0, elems = 0;
+};
+
+struct UnionFind {
+  std::vector<uint32_t> p;
+  explicit UnionFind(size_t n) : p(n) { std::iota(p.begin(), p.end(), 0u); }
+  uint32_t find(uint32_t x) {
+    while (p[x] != x) {
+      p[x] = p[p[x]];
+      x = p[x];
+    }
+    return x;
+  }
+  void join(uint32_t a, uint32_t b) {
+    a = find(a);
+    b = find(b);
+    if (a != b) p[std::max(a, b)] = std::min(a, b);
+  }
+};
+
+// Visits every update of passes [w0, w1) in order: f(level, left amplitude,
+// right amplitude, parity). False if a term is not an inline pair term or an
+// index is out of range.
+template <class F>
+bool for_each_update(const HostProgram& hp, const uint32_t* pool, size_t w0, size_t w1, F f) {
+  const uint32_t Ca = (uint32_t)hp.Ca, Cb = (uint32_t)hp.Cb;
+  uint32_t lv = 0;
+  for (size_t pi = w0; pi < w1; ++pi) {
+    const Pass& ps = hp.passes[pi];
+    for (uint32_t k = ps.op0; k < ps.op1; ++k, ++lv) {
+      const DevOp& d = hp.ops[k];
+      if (d.kind != OPK_PAIR || d.gen != OP_INLINE) return false;
+      for (uint32_t t = 0; t < ps.mixcount; ++t) {
+        const uint32_t pw = pool[ps.mixtab + 2 * t], b10 = pool[ps.mixtab + 2 * t + 1];
+        const uint32_t b01 = pw & 0x7fffffffu;
+        if (b01 >= Cb || b10 >= Cb) return false;
+        for (uint32_t j = 0; j < d.count; ++j) {
+          const uint32_t w = pool[d.tab + 2 * j], a01 = w & 0x7fffffffu, a10 = pool[d.tab + 2 * j + 1];
+          if (a01 >= Ca || a10 >= Ca) return false;
+          f(lv, a01 * Cb + b01, a10 * Cb + b10, (w >> 31) ^ (pw >> 31));
+        }
+      }
+    }
+  }
+  return true;
+}
+
+// The components of the window [w0, w1); false if it cannot be scheduled.
+bool window_components(const HostProgram& hp, const uint32_t* pool, size_t w0, size_t w1, uint32_t levels,
+                       std::vector<Comp>& comps) {
+  UnionFind uf((size_t)hp.Ca * hp.Cb);
+  if (!for_each_update(hp, pool, w0, w1, [&](uint32_t, uint32_t x, uint32_t y, uint32_t) { uf.join(x, y); }))
+    return false;
+  std::vector<int> cid(uf.p.size(), -1), lidx(uf.p.size(), -1);
+  comps.clear();
+  for_each_update(hp, pool, w0, w1, [&](uint32_t lv, uint32_t x, uint32_t y, uint32_t par) {
+    const uint32_t root = uf.find(x);
+    if (cid[root] < 0) {
+      cid[root] = (int)comps.size();
+      comps.emplace_back();
+      comps.back().lev.resize(levels);
+    }
+    Comp& c = comps[cid[root]];
+    for (uint32_t node : {x, y})
+      if (lidx[node] < 0) {
+        lidx[node] = (int)c.nodes.size();
+        c.nodes.push_back(node);
+      }
+    c.lev[lv].push_back({(uint32_t)lidx[x], (uint32_t)lidx[y], par});
+  });
+  for (Comp& c : comps)
+    for (const auto& l : c.lev) c.maxper = std::max<uint32_t>(c.maxper, (uint32_t)l.size());
+  return true;
+}
+
+// Team warps a unit of component c needs (0: too large for a group).
+uint32_t team_warps(const Comp& c) {
+  const uint32_t tw = std::max((c.maxper + kQuads - 1) / kQuads, ((uint32_t)c.nodes.size() + kLanes - 1) / kLanes);
+  return tw <= kMaxTeam ? std::max(tw, 1u) : 0u;
+}
+
+// Places the units of one window and writes its warp programs into `block`
+// (K * wpc programs of wp_words words). False if some unit does not fit.
+bool place_window(const HostProgram& hp, const std::vector<Comp>& comps, uint32_t op0, uint32_t levels, uint32_t K,
+                  uint32_t wpc, uint32_t stage_elems, uint32_t wp_words, uint32_t* block) {
+  const uint32_t groups = wpc / kMaxTeam;
+  std::vector<Team> teams;
+  // large units: one team each; small ones packed first-fit, largest first
+  std::vector<uint32_t> small;
+  for (uint32_t c = 0; c < comps.size(); ++c) {
+    const uint32_t tw = team_warps(comps[c]);
+    if (tw == 0) return false;
+    if (tw == 1) {
+      small.push_back(c);
+      continue;
+    }
+    Team tm;
+    tm.tw = tw;
+    tm.units.push_back(c);
+    tm.quads = comps[c].maxper;
+    tm.elems = (uint32_t)comps[c].nodes.size();
+    teams.push_back(tm);
+  }
+  std::stable_sort(teams.begin(), teams.end(), [](const Team& a, const Team& b) { return a.quads > b.quads; });
+  std::stable_sort(small.begin(), small.end(),
+                   [&](uint32_t a, uint32_t b) { return comps[a].maxper > comps[b].maxper; });
+  std::vector<Team> packs;
+  for (uint32_t c : small) {
+    const uint32_t q = comps[c].maxper, e = (uint32_t)comps[c].nodes.size();
+    bool placed = false;
+    for (Team& pk : packs)
+      if (pk.quads + q <= kQuads && pk.elems + e <= kLanes) {
+        pk.units.push_back(c);
+        pk.quads += q;
+        pk.elems += e;
+        placed = true;
+        break;
+      }
+    if (!placed) {
+      Team pk;
+      pk.units.push_back(c);
+      pk.quads = q;
+      pk.elems = e;
+      packs.push_back(pk);
+    }
+  }
+  teams.insert(teams.end(), packs.begin(), packs.end());
+  // CTA with the least quads per level that has room: a whole free group for a
+  // team of two or three warps, a free warp for one; stage room in that group.
+  std::vector<uint32_t> load(K, 0), gwarps((size_t)K * groups, 0), gstage((size_t)K * groups, 0);
+  std::fill(block, block + (size_t)K * wpc * wp_words, 0u);
+  const uint32_t Cb = (uint32_t)hp.Cb;
+  for (const Team& tm : teams) {
+    int best_cta = -1, best_grp = -1;
+    for (uint32_t r = 0; r < K; ++r) {
+      if (best_cta >= 0 && load[r] >= load[best_cta]) continue;
+      for (uint32_t g = 0; g < groups; ++g) {
+        const size_t gi = (size_t)r * groups + g;
+        const bool room = tm.tw > 1 ? gwarps[gi] == 0 : gwarps[gi] < kMaxTeam;
+        if (room && gstage[gi] + tm.elems <= stage_elems) {
+          best_cta = (int)r;
+          best_grp = (int)g;
+          break;
+        }
+      }
+    }
+    if (best_cta < 0) return false;
+    const size_t gi = (size_t)best_cta * groups + best_grp;
+    const uint32_t w0 = (uint32_t)best_grp * kMaxTeam + gwarps[gi];
+    const uint32_t ebase = gstage[gi];
+    gwarps[gi] += tm.tw;
+    gstage[gi] += tm.elems;
+    load[best_cta] += tm.quads;
+    if (ebase + tm.elems > kIdxLimit) return false;
+    // amplitudes: element i of the team goes to warp i / 32, lane i % 32, and to
+    // stage index ebase + i of the group; updates of level k: quad slot j goes to
+    // warp j / 8, quad j % 8
+    uint32_t* wp[kMaxTeam];
+    for (uint32_t w = 0; w < tm.tw; ++w) {
+      wp[w] = block + ((size_t)best_cta * wpc + w0 + w) * wp_words;
+      wp[w][0] = (tm.tw << 6) | (levels << 8);
+      wp[w][1] = op0;
+    }
+    uint32_t e0 = 0, q0 = 0;
+    for (uint32_t ci : tm.units) {
+      const Comp& c = comps[ci];
+      for (uint32_t i = 0; i < c.nodes.size(); ++i) {
+        const uint32_t row = c.nodes[i] / Cb, col = c.nodes[i] % Cb, e = e0 + i;
+        uint32_t* w = wp[e / kLanes];
+        w[kMixWpHeader + e % kLanes] = row | (col << 11) | ((ebase + e) << 22);
+        w[0] = (w[0] & ~63u) | ((w[0] & 63u) + 1);
+      }
+      for (uint32_t k = 0; k < levels; ++k)
+        for (uint32_t j = 0; j < c.lev[k].size(); ++j) {
+          const Upd& up = c.lev[k][j];
+          const uint32_t slot = q0 + j;
+          wp[slot / kQuads][kMixWpHeader + kLanes + kQuads * k + slot % kQuads] =
+              (ebase + e0 + up.l) | ((ebase + e0 + up.r) << 10) | (up.par << 20) | (1u << 21);
+        }
+      e0 += (uint32_t)c.nodes.size();
+      q0 += c.maxper;
+    }
+  }
+  return true;
+}
+
+}  // namespace
+
+uint32_t mix_wp_words(const HostProgram&) { return (kMixWpHeader + kLanes + kQuads * kMixMaxLevels + 3) & ~3u; }
+
+bool build_mix_units(const HostProgram& hp, const uint32_t* pool, uint32_t K, uint32_t warps_per_cta,
+                     uint32_t stage_elems, uint32_t max_window, MixUnits& out) {
+  out = MixUnits{};
+  if (hp.Ca >= kLineLimit || hp.Cb >= kLineLimit || K == 0 || warps_per_cta < kMaxTeam || max_window == 0)
+    return false;
+  if (hp.Ca * hp.Cb > (1u << 22)) return false;  // the union-find runs over the block's amplitudes
+  const uint32_t full = mix_wp_words(hp);
+  const size_t block = (size_t)K * warps_per_cta * full;
+  out.warps_per_cta = warps_per_cta;
+  out.cluster = K;
+  out.pass_slot.assign(hp.passes.size(), kMixNoSchedule);
+  struct Window {
+    size_t w0, w1;
+    uint32_t levels;
+    std::vector<uint32_t> words;  // K * wpc programs of `full` words
+  };
+  std::vector<Window> wins;
+  std::vector<Comp> comps;
+  std::vector<uint32_t> trial(block);
+  auto mixable = [&](size_t pi) {
+    const Pass& p = hp.passes[pi];
+    return p.type == PASS_MIX && p.op1 > p.op0 && p.mixcount > 0;
+  };
+  size_t pi = 0;
+  while (pi < hp.passes.size()) {
+    if (!mixable(pi)) {
+      ++pi;
+      continue;
+    }
+    // grow [pi, end) one pass at a time while the window still schedules
+    Window best{pi, pi, 0, {}};
+    uint32_t levels = 0;
+    for (size_t end = pi + 1; end <= hp.passes.size() && end - pi <= max_window; ++end) {
+      if (!mixable(end - 1)) break;
+      levels += hp.passes[end - 1].op1 - hp.passes[end - 1].op0;
+      if (levels > kMixMaxLevels) break;
+      if (!window_components(hp, pool, pi, end, levels, comps)) break;
+      if (!place_window(hp, comps, hp.passes[pi].op0, levels, K, warps_per_cta, stage_elems, full, trial.data()))
+        break;
+      best.w1 = end;
+      best.levels = levels;
+      best.words = trial;
+    }
+    if (best.w1 == pi) {
+      ++pi;  // this pass runs by tiles
+      continue;
+    }
+    pi = best.w1;
+    wins.push_back(std::move(best));
+  }
+  if (wins.empty()) return false;
+  // the programs at the size the longest window needs
+  uint32_t lmax = 1;
+  for (const Window& w : wins) lmax = std::max(lmax, w.levels);
+  out.wp_words = (kMixWpHeader + kLanes + kQuads * lmax + 3) & ~3u;
+  const size_t progs = (size_t)K * warps_per_cta;
+  out.words.assign(wins.size() * progs * out.wp_words, 0u);
+  for (size_t wi = 0; wi < wins.size(); ++wi) {
+    for (size_t p = 0; p < progs; ++p)
+      std::copy_n(wins[wi].words.data() + p * full, out.wp_words, out.words.data() + (wi * progs + p) * out.wp_words);
+    const uint32_t span = (uint32_t)(wins[wi].w1 - wins[wi].w0);
+    for (size_t q = wins[wi].w0; q < wins[wi].w1; ++q) out.pass_slot[q] = (uint32_t)wi | (span << 20);
+    out.scheduled += span;
+  }
+  out.windows = (uint32_t)wins.size();
+  return true;
+}
+
+}  // namespace qpe

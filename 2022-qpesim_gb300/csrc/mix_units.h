@@ -1,0 +1,69 @@
+// mix_units.h - runs of column-pair (MIX) passes as independent update units, for
+// the resident kernel with the block spread over a cluster (k_resident_lean).
+//
+// Every term of a MIX pass pairs amplitude (a, b01) with (a', b10) for each row
+// pair (a, a') of its alpha table and each column pair (b01, b10) of the pass's
+// beta table. Take a window of consecutive MIX passes and join the two amplitudes
+// of every such pair: the window's updates split into connected components, and
+// updates of different components touch disjoint amplitudes. So a component (a
+// "unit") can run on its own for the whole window: gather its amplitudes, apply
+// the window's terms in order (level k = the window's term k; within a level every
+// update is on its own pair of amplitudes), scatter them back. The updates that
+// touch one amplitude keep their order and each keeps the tile runner's
+// arithmetic, so the results are bit-identical; a window of w passes needs one
+// gather, one scatter and one cluster barrier instead of w of each.
+//
+// The host grows each window while its units still fit (at most 24 updates per
+// level and 96 amplitudes per unit; the kernel's warps and stages) and packs the
+// units into warp programs: small units share a warp (each on its own quads of
+// lanes and its own range of the group's stage), large ones take a team of two
+// or three warps of one three-warp group, which then synchronises by the group's
+// named barrier. Units go to the CTA with the least work per level.
+//
+// Per pass (MixUnits::pass_slot): kMixNoSchedule (the pass runs by tiles), or the
+// window's block of warp programs (bits 0-19) and its number of passes (bits
+// 20-27), the same for every pass of the window. A sweep meets a window at its
+// first pass (forward) or its last (reversed), runs it, and skips its other passes.
+//
+// Warp program (kMixWpHeader + 32 + 8 * levels words, a multiple of 4):
+//   w[0]                     nelem (bits 0-5, <= 32) | team warps (bits 6-7; 0: idle)
+//                            | levels (bits 8-15)
+//   w[1]                     first term of the window (its op index)
+//   w[kMixWpHeader + l]      gather entry of lane l: row | col << 11 | stage index << 22
+//   w[kMixWpHeader + 32 + 8 k + u]
+//                            update of quad u at level k: left stage index
+//                            | right stage index << 10 | parity << 20 | valid << 21
+#ifndef QPE_MIX_UNITS_H_
+#define QPE_MIX_UNITS_H_
+
+#include <stdint.h>
+
+#include <vector>
+
+#include "program_build.h"
+
+namespace qpe {
+
+struct MixUnits {
+  uint32_t wp_words = 0;             // words per warp program
+  uint32_t warps_per_cta = 0;
+  uint32_t cluster = 0;
+  uint32_t scheduled = 0;            // MIX passes with a schedule
+  uint32_t windows = 0;              // blocks of warp programs
+  std::vector<uint32_t> pass_slot;   // per pass, as above
+  std::vector<uint32_t> words;       // blocks [window][cta][warp][wp_words]
+};
+
+// Words of one warp program (windows of at most kMixMaxLevels terms).
+uint32_t mix_wp_words(const HostProgram& hp);
+
+// Builds the windows and unit schedules of the MIX passes of `hp` whose terms are
+// inline pair terms, windows of at most max_window passes. `pool` is the
+// program's index pool as built on the device. Passes whose units do not fit keep
+// the tile runner. Returns false when no pass could be scheduled.
+bool build_mix_units(const HostProgram& hp, const uint32_t* pool, uint32_t K, uint32_t warps_per_cta,
+                     uint32_t stage_elems, uint32_t max_window, MixUnits& out);
+
+}  // namespace qpe
+
+#endif  // QPE_MIX_UNITS_H_

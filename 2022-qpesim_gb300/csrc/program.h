@@ -71,6 +71,13 @@ enum PassType : uint8_t { PASS_COL = 0, PASS_ROW = 1, PASS_MIX = 2 };
 constexpr uint32_t kPairChunk = 4;
 constexpr uint32_t kPairTrips = 3;
 
+// Column-pair passes as update units (mix_units.h): words before a warp
+// program's gather entries, the most terms a scheduled window may have, and the
+// slot of a pass without a schedule.
+constexpr uint32_t kMixWpHeader = 4;
+constexpr uint32_t kMixMaxLevels = 24;
+constexpr uint32_t kMixNoSchedule = 0xffffffffu;
+
 struct Pass {
   uint32_t type;
   uint32_t op0, op1;

@@ -491,6 +491,15 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
     rowp[a] = cta_ptr(blk, r, K) + (size_t)(a - r * Rk) * Cb;
   }
   auto at = [&](uint32_t a, uint32_t b) -> C2* { return rowp[a] + b; };
+  // Column-pair update units (mix_units.h): this warp's program slot follows the
+  // row-pointer table; the slot holds the program of window wp_pass (or its copy
+  // on the way, cp.async).
+  const uint32_t wpw = (K > 1 && I.mix_words) ? I.mix_wp_words : 0u;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  unsigned char* const wp_base =
+      smem_raw + ((head + 15) & ~(size_t)15) + (((size_t)Ca * sizeof(C2*) + 15) & ~(size_t)15);
+  uint32_t* const wp_s = reinterpret_cast<uint32_t*>(wp_base) + (size_t)warp * wpw;
+  uint32_t wp_pass = kMixNoSchedule;
 
   const DevOp* ops = I.ops;
   const uint32_t* pool = I.pool;
@@ -498,8 +507,7 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
   const uint32_t* strA = I.strA;
   const uint32_t* strB = I.strB;
   if constexpr (MS)
-    stage_program(I, smem_raw + ((head + 15) & ~(size_t)15) + (((size_t)Ca * sizeof(C2*) + 15) & ~(size_t)15), ops,
-                  pool, passes, strA, strB);
+    stage_program(I, wp_base + (size_t)wpc * wpw * 4, ops, pool, passes, strA, strB);
   constexpr bool G = !MS;
   constexpr int kDepth = sizeof(R) == 8 ? 2 : 4;
   const bool in_group = grp < ngrp;  // threads past the last whole group only join the CTA barriers
@@ -511,14 +519,80 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
   barrier();
 
   const uint32_t nsweeps = I.steps * I.order;
+  // per pass: kMixNoSchedule, or its window's block of warp programs (bits 0-19)
+  // and the window's passes (bits 20-27)
+  auto mix_slot = [&](uint32_t pi) { return wpw ? __ldg(I.mix_slot + pi) : kMixNoSchedule; };
+  // Copies this warp's program of the window of pass pi (if it has one) into its
+  // slot; every lane of the warp calls it. A copy still on its way is waited for
+  // first.
+  auto wp_fetch = [&](uint32_t pi) {
+    const uint32_t m = mix_slot(pi);
+    if (m == kMixNoSchedule || wp_pass == (m & 0xfffffu)) return;
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncwarp();
+    const uint32_t* src = I.mix_words + (((size_t)(m & 0xfffffu) * K + rank) * wpc + warp) * wpw;
+    for (uint32_t c = lane; c < wpw / 4; c += 32) {
+      const uint32_t d = (uint32_t)__cvta_generic_to_shared(wp_s + 4 * c);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src + 4 * c) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    wp_pass = m & 0xfffffu;
+  };
+  auto pass_at = [&](uint32_t sw, uint32_t pj) { return (I.order == 2 && (sw & 1)) ? I.npasses - 1 - pj : pj; };
   for (uint32_t k = I.first; k < I.last; ++k) {
     for (uint32_t sw = 0; sw < nsweeps; ++sw) {
       const bool rev = I.order == 2 && (sw & 1);
       for (uint32_t pj = 0; pj < I.npasses; ++pj) {
         const uint32_t pi = rev ? I.npasses - 1 - pj : pj;
         const Pass P = passes[pi];
+        const uint32_t m = P.type == PASS_MIX ? mix_slot(pi) : kMixNoSchedule;
+        // a window of w passes is met at its first pass in either direction (the
+        // passes are consecutive) and runs them all: the loop skips the rest
+        const uint32_t span = m == kMixNoSchedule ? 1u : (m >> 20) & 0xffu;
+        const uint32_t nj = pj + span;
+        const uint32_t next_pi = nj < I.npasses ? pass_at(sw, nj) : pass_at(sw + 1 < nsweeps ? sw + 1 : 0, 0);
         if (!in_group) {
           // no tile
+        } else if (m != kMixNoSchedule) {
+          // this warp's share of the window's update units: gather its amplitudes
+          // into the group's stage, one level per term (quad u of the warp does
+          // update u of the level, split over its four lanes as in the tile
+          // runner), scatter them back
+          wp_fetch(pi);
+          asm volatile("cp.async.wait_all;" ::: "memory");
+          __syncwarp();
+          const uint32_t hdr = wp_s[0], op0 = wp_s[1];
+          const uint32_t tw = (hdr >> 6) & 3u;
+          if (tw) {
+            auto tsync = [&]() {
+              if (tw == 1) __syncwarp();
+              else asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(32 * tw) : "memory");
+            };
+            C2* const gst = blk + (size_t)Rk * Cb + (size_t)grp * stage_elems;
+            const uint32_t nel = hdr & 63u, nlev = (hdr >> 8) & 0xffu;
+            const uint32_t gw = lane < nel ? wp_s[kMixWpHeader + lane] : 0u;
+            C2* const gp = at(gw & 2047u, (gw >> 11) & 2047u);
+            C2* const sp = gst + (gw >> 22);
+            if (lane < nel) *sp = *gp;
+            tsync();
+            const uint32_t q = lane & 3u, quad = lane >> 2;
+            const bool side1 = q >= 2;
+            const uint32_t comp1 = q & 1u, sflip = comp1 ^ 1u;
+            R* const gr = reinterpret_cast<R*>(gst);
+            for (uint32_t i = 0; i < nlev; ++i) {
+              const uint32_t lv = rev ? nlev - 1 - i : i;
+              const uint32_t uw = wp_s[kMixWpHeader + 32 + 8 * lv + quad];
+              const uint4 b = ldm<G>(reinterpret_cast<const uint4*>(ops + op0 + lv) + 1);
+              const R c = (R)__hiloint2double((int)b.y, (int)b.x), t = (R)__hiloint2double((int)b.w, (int)b.z);
+              const bool v = (uw >> 21) & 1u;
+              R* const dp = gr + 2 * (side1 ? ((uw >> 10) & 1023u) : (uw & 1023u)) + comp1;
+              const R x1 = v ? *dp : (R)0;
+              const R x2 = __shfl_xor_sync(0xffffffffu, x1, 3);
+              if (v) *dp = A::add(A::mul(x1, c), A::mul(x2, (((uw >> 20) & 1u) ^ sflip) ? neg(t) : t));
+              tsync();
+            }
+            if (lane < nel) *gp = *sp;
+          }
         } else if (P.type == PASS_ROW) {
           // this CTA's rows, one per group tile, in place
           for (uint32_t r = row0 + grp; r < row1; r += ngrp) {
@@ -572,13 +646,16 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
             }
           }
         }
+        if (in_group) wp_fetch(next_pi);
         barrier();
+        pj += span - 1;
       }
     }
     C2* dst = gstate + (uint64_t)(I.in_place ? I.first : k) * ld + (uint64_t)row0 * Cb;
     for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) dst[i] = blk[i];
     barrier();
   }
+  asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 template <typename R, class A, bool MS>

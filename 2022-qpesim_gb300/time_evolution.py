@@ -96,6 +96,13 @@ class Program:
     def touches_per_power(self) -> int:
         return int(self.info["touches_per_power"])
 
+    def unit_schedule(self) -> tuple:
+        """(cluster size, column-pair passes scheduled) of the update-unit schedule
+        the program last built for strategy 7 (qpe_program_unit_schedule)."""
+        k, n = C.c_uint32(), C.c_uint32()
+        N.check(self._lib.qpe_program_unit_schedule(self._h, C.byref(k), C.byref(n)))
+        return int(k.value), int(n.value)
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:

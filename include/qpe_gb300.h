@@ -209,6 +209,10 @@ int qpe_program_plan(uint32_t num_orbitals, uint32_t n_alpha, uint32_t n_beta, c
                      size_t n_pqqr, const qpe_term* pqrs, size_t n_pqrs, uint32_t trotter_order,
                      uint32_t steps_per_power, qpe_program_info* info);
 int qpe_program_get_info(const qpe_program* prog, qpe_program_info* info);
+/* The column-pair update-unit schedule (QPE_STRATEGY_LEAN_UNITS) the program last
+ * built: its cluster size and how many column-pair passes it schedules (the rest
+ * run as tiles); 0, 0 before any evolution with that strategy. */
+int qpe_program_unit_schedule(const qpe_program* prog, uint32_t* cluster_size, uint32_t* scheduled_passes);
 
 int qpe_state_create(qpe_context* ctx, uint32_t num_orbitals, uint32_t n_alpha, uint32_t n_beta,
                      uint32_t precision, int dtype, qpe_state** out);
@@ -230,6 +234,11 @@ int qpe_state_zero(qpe_state* st);
 #define QPE_STRATEGY_LEAN 6     /* as CLUSTER (cluster_size 1..16): every row, column or column
                                    pair processed by a three-warp group, pair updates split over
                                    four lanes and diagonal updates over two */
+#define QPE_STRATEGY_LEAN_UNITS 7 /* as LEAN (cluster_size 2..16), with each column-pair pass split
+                                     into the connected components of its row pairings per column
+                                     pair, packed into warps by a host schedule: no CTA runs two
+                                     column pairs while others idle, and a warp synchronises with
+                                     itself between terms instead of with its group */
 
 /* complex128 only: allow fused multiply-adds. Results then differ from the
  * reference's rounding by a few ulps per update (within 1e-12 of it) instead of

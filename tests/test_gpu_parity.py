@@ -223,7 +223,8 @@ def test_pp_fixture_phase_on_gpu(gpu):
 @pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 2), (2, 4), (2, 8), (2, 16), (3, 0), (0, 0),
                                               (4, 1), (4, 2), (4, 4), (4, 8), (4, 16),
                                               (5, 1), (5, 2), (5, 4), (5, 8), (5, 16),
-                                              (6, 1), (6, 2), (6, 4), (6, 8), (6, 16)])
+                                              (6, 1), (6, 2), (6, 4), (6, 8), (6, 16),
+                                              (7, 2), (7, 4), (7, 8), (7, 16)])
 @pytest.mark.parametrize("n,na,nb,P", [(12, 3, 3, 3), (14, 4, 3, 2), (8, 2, 2, 4), (16, 4, 4, 2)])
 def test_strategies_bit_identical(gpu, orc, strategy, cluster, n, na, nb, P):
     """Every evolution strategy (one CTA resident in shared memory, clusters of 2
@@ -245,7 +246,7 @@ def test_strategies_bit_identical(gpu, orc, strategy, cluster, n, na, nb, P):
     assert np.array_equal(st.download(), ref)
 
 
-@pytest.mark.parametrize("strategy,cluster", [(0, 0), (6, 16), (6, 8), (3, 0)])
+@pytest.mark.parametrize("strategy,cluster", [(0, 0), (6, 16), (6, 8), (7, 16), (7, 8), (3, 0)])
 def test_headline_configuration(gpu, orc, strategy, cluster):
     """The plain-n16 bench workload exactly as it is timed, at P = 3: n = 16,
     N = 8, seed-0 integrals, 2nd-order Trotter (forward and reversed sweeps at
@@ -265,8 +266,11 @@ def test_headline_configuration(gpu, orc, strategy, cluster):
     b0 = q.hf_block0(st.c_alpha, st.c_beta, P)
     st.upload(b0)
     st.evolve(prog, strategy=strategy, cluster_size=cluster)
-    if strategy == 6:
-        assert st.last_strategy() == (6, cluster)
+    if strategy in (6, 7):
+        assert st.last_strategy() == (strategy, cluster)
+    if strategy == 7:
+        # every one of the 392 column-pair passes of a sweep as update units
+        assert prog.unit_schedule() == (cluster, 392)
     ref = np.zeros(st.size, np.complex128)
     ref[:st.ld] = b0
     orc.time_evolve(M, e, e, P, seg, ref, order=order, steps=steps)
@@ -278,7 +282,8 @@ def test_headline_configuration(gpu, orc, strategy, cluster):
                                atol=1e-16)
 
 
-@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0), (4, 1), (4, 4), (5, 1), (5, 4), (6, 1), (6, 4)])
+@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0), (4, 1), (4, 4), (5, 1), (5, 4), (6, 1), (6, 4),
+                                              (7, 4), (7, 16)])
 def test_strategies_complex64(gpu, orc, strategy, cluster):
     q = gpu
     n, N, P = 12, 6, 4
@@ -295,7 +300,7 @@ def test_strategies_complex64(gpu, orc, strategy, cluster):
     assert np.abs(st.download() - ref).max() < 2e-5
 
 
-@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0), (4, 1), (4, 4), (5, 4), (6, 4)])
+@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 4), (3, 0), (4, 1), (4, 4), (5, 4), (6, 4), (7, 4)])
 def test_fp64_contract_within_tolerance(gpu, orc, strategy, cluster):
     """With FMAs allowed (QPE_EVOLVE_FP64_CONTRACT) complex128 stays within 1e-12
     of the reference's rounding (here over 15 powers of a 2nd-order, 2-step
@@ -387,7 +392,7 @@ def test_batch_complex64_eigenphase_matches_fp64(gpu):
 
 
 @pytest.mark.parametrize("name", sorted(p.name for p in GOLDEN.glob("iqpe_*.npz")))
-@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 2), (3, 0), (0, 0), (4, 2), (5, 2), (6, 2)])
+@pytest.mark.parametrize("strategy,cluster", [(1, 0), (2, 2), (3, 0), (0, 0), (4, 2), (5, 2), (6, 2), (7, 4)])
 def test_iqpe_golden(gpu, name, strategy, cluster):
     """time_evolve_iqpe (cpp/time_evolution_over_terms.hpp:141-155): block 1 in
     place, applyUnitary's term order, against the reference's own output, through
@@ -423,7 +428,8 @@ def test_iqpe_bit_identical_to_oracle(gpu, orc, strategy):
     assert np.array_equal(st.download(), reg)
 
 
-@pytest.mark.parametrize("strategy,order,steps", [(1, 1, 1), (2, 2, 2), (3, 2, 1), (4, 2, 2), (5, 2, 2), (6, 2, 2)])
+@pytest.mark.parametrize("strategy,order,steps", [(1, 1, 1), (2, 2, 2), (3, 2, 1), (4, 2, 2), (5, 2, 2), (6, 2, 2),
+                                                   (7, 2, 2)])
 def test_in_place_repeats_equal_powers(gpu, strategy, order, steps):
     """r in-place applications to block 1 holding block 0 give block r of the
     ordinary controlled-power evolution, bit for bit, in any strategy."""
