@@ -420,7 +420,7 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
 }
 
 // Most consecutive column-pair passes one window of update units may take.
-constexpr uint32_t kMixWindowPasses = 4;
+constexpr uint32_t kMixWindowPasses = 8;
 
 // The column-pair update-unit schedule of `pr` for cluster K, wpc warps per CTA
 // and group stages of `stage` elements, built from the device's index pool on

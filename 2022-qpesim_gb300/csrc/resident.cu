@@ -579,10 +579,18 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
             const bool side1 = q >= 2;
             const uint32_t comp1 = q & 1u, sflip = comp1 ^ 1u;
             R* const gr = reinterpret_cast<R*>(gst);
+            // the next level's update word and coefficients are loaded a level ahead
+            uint32_t lv_n = rev ? nlev - 1 : 0;
+            uint32_t uw_n = wp_s[kMixWpHeader + 32 + 8 * lv_n + quad];
+            uint4 b_n = ldm<G>(reinterpret_cast<const uint4*>(ops + op0 + lv_n) + 1);
             for (uint32_t i = 0; i < nlev; ++i) {
-              const uint32_t lv = rev ? nlev - 1 - i : i;
-              const uint32_t uw = wp_s[kMixWpHeader + 32 + 8 * lv + quad];
-              const uint4 b = ldm<G>(reinterpret_cast<const uint4*>(ops + op0 + lv) + 1);
+              const uint32_t uw = uw_n;
+              const uint4 b = b_n;
+              if (i + 1 < nlev) {
+                lv_n = rev ? nlev - 2 - i : i + 1;
+                uw_n = wp_s[kMixWpHeader + 32 + 8 * lv_n + quad];
+                b_n = ldm<G>(reinterpret_cast<const uint4*>(ops + op0 + lv_n) + 1);
+              }
               const R c = (R)__hiloint2double((int)b.y, (int)b.x), t = (R)__hiloint2double((int)b.w, (int)b.z);
               const bool v = (uw >> 21) & 1u;
               R* const dp = gr + 2 * (side1 ? ((uw >> 10) & 1023u) : (uw & 1023u)) + comp1;

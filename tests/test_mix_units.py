@@ -1,0 +1,69 @@
+"""The column-pair update-unit scheduler (csrc/mix_units.cpp, strategy 7), on the
+CPU: tests/units/mix_units_check.cc runs every scheduled window of a program both
+the tile runner's way and the warp programs' way on a random complex128 block and
+counts differences (bit for bit) and broken kernel invariants (team layout,
+bounds, one owner per stage index and per amplitude). The GPU parity tests run
+the same schedules in k_resident_lean against the oracle."""
+import ctypes as C
+import math
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+CSRC = ROOT / "2022-qpesim_gb300" / "csrc"
+KINDS = ("pp", "pq", "pqqp", "pqqr", "pqrs")
+
+
+@pytest.fixture(scope="module")
+def checker(tmp_path_factory):
+    out = tmp_path_factory.mktemp("units") / "libmix_units_check.so"
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-shared", "-fPIC", f"-I{CSRC}", f"-I{ROOT / 'include'}",
+           str(ROOT / "tests" / "units" / "mix_units_check.cc"), str(CSRC / "mix_units.cpp"),
+           str(CSRC / "program_build.cpp"), "-o", str(out)]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    lib = C.CDLL(str(out))
+    lib.mix_units_check.restype = C.c_int
+    lib.mix_units_check.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_uint, C.c_uint,
+                                    C.c_uint, C.c_uint, C.c_uint, C.POINTER(C.c_uint)]
+    return lib
+
+
+def _run(q, lib, n, K, order, wpc, max_window, seed=0):
+    M, e = n // 2, n // 4
+    h = q.Hamiltonian.from_integrals(q.synthetic_integrals(n, seed), e, 0.05)
+    seg = h.segmented_terms()
+    arrs = [np.ascontiguousarray(seg[k], dtype=q._native.TERM_DTYPE) for k in KINDS]
+    ptrs = (C.c_void_p * 5)(*[a.ctypes.data for a in arrs])
+    ns = (C.c_size_t * 5)(*[len(a) for a in arrs])
+    stats = (C.c_uint * 4)()
+    bad = lib.mix_units_check(M, e, e, ptrs, ns, order, K, wpc, 2 * math.comb(M, e), max_window, stats)
+    return bad, dict(scheduled=stats[0], windows=stats[1], wp_words=stats[2], max_quads=stats[3])
+
+
+def test_headline_schedule(q, checker):
+    """n = 16, N = 8, cluster of 16, 15 warps per CTA, windows of up to 4 passes
+    (the headline configuration): every one of the 392 column-pair passes is
+    scheduled, in fewer windows, and the unit runs equal the tile runs bit for bit."""
+    bad, st = _run(q, checker, 16, 16, 2, 15, 4)
+    assert bad == 0
+    assert st["scheduled"] == 392
+    assert st["windows"] < 392 // 2
+    assert st["max_quads"] <= 40  # the most update slots one CTA runs at one level
+
+
+@pytest.mark.parametrize("n,K,order,wpc,max_window", [(16, 16, 1, 15, 1), (16, 8, 1, 15, 4), (16, 8, 2, 9, 2),
+                                                      (12, 16, 1, 15, 4), (12, 4, 2, 15, 2), (14, 16, 1, 9, 4),
+                                                      (10, 4, 1, 6, 3), (8, 2, 1, 15, 4), (16, 2, 2, 15, 4)])
+def test_schedules_equal_tile_runs(q, checker, n, K, order, wpc, max_window):
+    bad, st = _run(q, checker, n, K, order, wpc, max_window, seed=n)
+    assert bad == 0, st
+
+
+def test_units_too_large_fall_back(q, checker):
+    """n = 20 (70 row pairs per term and column pair): no unit fits a three-warp
+    group, so no pass is scheduled and every column-pair pass keeps the tiles."""
+    bad, st = _run(q, checker, 20, 16, 1, 15, 4)
+    assert bad == 0 and st["scheduled"] == 0 and st["windows"] == 0
