@@ -44,7 +44,8 @@ class ProgramInfo(C.Structure):
 
 class EvolveOpts(C.Structure):
     _fields_ = [("strategy", C.c_uint32), ("first_power", C.c_uint32), ("last_power", C.c_uint32),
-                ("cluster_size", C.c_uint32), ("flags", C.c_uint32), ("repeats", C.c_uint32)]
+                ("cluster_size", C.c_uint32), ("flags", C.c_uint32), ("repeats", C.c_uint32),
+                ("replicas", C.c_uint32)]
 
 
 QPE_EVOLVE_FP64_CONTRACT, QPE_EVOLVE_IN_PLACE = 1, 2
@@ -103,6 +104,7 @@ PROTOTYPES = {
     "qpe_state_phase_probs": (C.c_int, [_vp, _PD]),
     "qpe_state_block_norms": (C.c_int, [_vp, _PD]),
     "qpe_state_last_strategy": (C.c_int, [_vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "qpe_state_last_replicas": (C.c_int, [_vp, C.POINTER(C.c_uint32)]),
     # host-side term compiler
     # learned initial-state model
     "qpe_mlp_create": (C.c_int, [_vp, C.c_uint32, C.c_uint32, C.c_uint64, C.POINTER(_vp)]),

@@ -40,8 +40,10 @@ struct qpe_state {
   DevBuf res_inst;
   uint64_t tuned_prog = 0;
   uint32_t tuned_exact = 1;
-  uint32_t tuned_strategy = 0, tuned_cluster = 0;
-  uint32_t last_strategy = 0, last_cluster = 0;
+  uint32_t tuned_strategy = 0, tuned_cluster = 0, tuned_replicas = 1;
+  uint32_t last_strategy = 0, last_cluster = 0, last_replicas = 1;
+  // Replica exchange of the lean kernel (ResidentInstance::xbuf, xflag).
+  DevBuf xbuf, xflag;
   ~qpe_state() {
     if (graph) cudaGraphExecDestroy(graph);
   }
@@ -217,8 +219,9 @@ void check_device_error(qpe_context* ctx) {
   if (e) {
     QPE_CK(cudaMemsetAsync(ctx->err.p, 0, sizeof(int), ctx->stream));
     QPE_CK(cudaStreamSynchronize(ctx->stream));
-    throw Error(QPE_ERR_TIMEOUT, "a tile pass's bounded wait for its bulk copies ran out (code " + std::to_string(e) +
-                                     "); the affected results are invalid");
+    throw Error(QPE_ERR_TIMEOUT, "a kernel's bounded wait ran out (code " + std::to_string(e) +
+                                     ": 2 a tile pass's bulk copies, 4 another replica's exchange); the "
+                                     "affected results are invalid");
   }
 }
 
@@ -421,6 +424,8 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
 
 // Most consecutive column-pair passes one window of update units may take.
 constexpr uint32_t kMixWindowPasses = 8;
+// Replica clusters a lean launch may have (QPE_STRATEGY_LEAN_UNITS).
+constexpr uint32_t kMaxReplicas = 4;
 
 // The column-pair update-unit schedule of `pr` for cluster K, wpc warps per CTA
 // and group stages of `stage` elements, built from the device's index pool on
@@ -453,11 +458,24 @@ static bool ensure_mix_units(const qpe_program* pr, uint32_t K, uint32_t wpc, ui
 }
 
 static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint32_t first, uint32_t last,
-                         bool exact, bool in_place = false, uint32_t mode = 0) {
+                         bool exact, bool in_place = false, uint32_t mode = 0, uint32_t replicas = 1) {
   ResidentLaunch rl;
   ResidentInstance ri{};
   if (!plan_resident(pr, st, K, rl, ri, mode))
     throw Error(QPE_ERR_UNSUPPORTED, "block does not fit the cluster's shared memory");
+  if (replicas > 1) {
+    // replica clusters of the lean kernel, each holding the whole block
+    if (rl.group != 3 || K < 2) throw Error(QPE_ERR_INVALID, "replicas need a three-warp-group cluster of 2 or more");
+    if (replicas > kMaxReplicas) throw Error(QPE_ERR_INVALID, "at most 4 replicas");
+    if (st->xbuf.bytes < 2 * st->ld * st->esz) st->xbuf.alloc(2 * st->ld * st->esz);
+    if (!st->xflag.p) st->xflag.alloc(16 * kMaxReplicas * sizeof(uint32_t));
+    QPE_CK(cudaMemsetAsync(st->xflag.p, 0, st->xflag.bytes, st->ctx->stream));
+    rl.replicas = replicas;
+    ri.replicas = replicas;
+    ri.xbuf = st->xbuf.p;
+    ri.xflag = st->xflag.as<uint32_t>();
+  }
+  ri.err = st->ctx->err.as<int>();
   if (mode == 4 && ensure_mix_units(pr, K, rl.warps_per_cta, rl.stage_elems)) {
     ri.mix_words = pr->mix_words.as<uint32_t>();
     ri.mix_slot = pr->mix_slot.as<uint32_t>();
@@ -502,9 +520,10 @@ static uint32_t resident_mode(uint32_t strategy) {
 
 // Strategy for (program, state): explicit, or timed on one power per candidate.
 static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts, bool exact,
-                            uint32_t& strategy, uint32_t& K) {
+                            uint32_t& strategy, uint32_t& K, uint32_t& replicas) {
   strategy = opts ? opts->strategy : QPE_STRATEGY_AUTO;
   K = opts ? opts->cluster_size : 0;
+  replicas = (opts && opts->replicas && strategy == QPE_STRATEGY_LEAN_UNITS) ? opts->replicas : 1u;
   ResidentLaunch rl;
   ResidentInstance ri{};
   if (strategy == QPE_STRATEGY_RESIDENT) {
@@ -525,6 +544,7 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
   if (st->tuned_prog == pr->id && st->tuned_exact == (uint32_t)exact) {
     strategy = st->tuned_strategy;
     K = st->tuned_cluster;
+    replicas = st->tuned_replicas;
     return;
   }
   // Autotune: time one power of every feasible candidate, the tiled strategy
@@ -538,16 +558,21 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     void* dst; const void* src; size_t n; cudaStream_t s;
     ~Restore() { cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, s); cudaStreamSynchronize(s); }
   } restore{block1, saved.p, st->ld * st->esz, st->ctx->stream};
-  std::vector<std::pair<uint32_t, uint32_t>> cands;
+  struct Cand {
+    uint32_t strategy, K, replicas;
+  };
+  std::vector<Cand> cands;
   for (uint32_t c = 1; c <= 16; c *= 2) {
-    if (plan_resident(pr, st, c, rl, ri)) cands.push_back({c == 1 ? QPE_STRATEGY_RESIDENT : QPE_STRATEGY_CLUSTER, c});
-    if (plan_resident(pr, st, c, rl, ri, 1)) cands.push_back({QPE_STRATEGY_GROUP, c});
-    if (plan_resident(pr, st, c, rl, ri, 2)) cands.push_back({QPE_STRATEGY_HYBRID, c});
-    if (plan_resident(pr, st, c, rl, ri, 3)) cands.push_back({QPE_STRATEGY_LEAN, c});
+    const uint32_t one = 1;
+    if (plan_resident(pr, st, c, rl, ri))
+      cands.push_back({c == 1 ? (uint32_t)QPE_STRATEGY_RESIDENT : (uint32_t)QPE_STRATEGY_CLUSTER, c, one});
+    if (plan_resident(pr, st, c, rl, ri, 1)) cands.push_back({(uint32_t)QPE_STRATEGY_GROUP, c, one});
+    if (plan_resident(pr, st, c, rl, ri, 2)) cands.push_back({(uint32_t)QPE_STRATEGY_HYBRID, c, one});
+    if (plan_resident(pr, st, c, rl, ri, 3)) cands.push_back({(uint32_t)QPE_STRATEGY_LEAN, c, one});
     if (plan_resident(pr, st, c, rl, ri, 4) && ensure_mix_units(pr, c, rl.warps_per_cta, rl.stage_elems))
-      cands.push_back({QPE_STRATEGY_LEAN_UNITS, c});
+      for (uint32_t r = 1; r <= (c >= 8 ? 3u : 1u); ++r) cands.push_back({(uint32_t)QPE_STRATEGY_LEAN_UNITS, c, r});
   }
-  cands.push_back({QPE_STRATEGY_TILED, 0});
+  cands.push_back({(uint32_t)QPE_STRATEGY_TILED, 0u, 1u});
   if (cands.size() == 1) {
     strategy = QPE_STRATEGY_TILED;
   } else {
@@ -558,8 +583,9 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     for (auto& c : cands) {
       float ms = 0;
       auto run = [&]() {
-        if (c.first == QPE_STRATEGY_TILED) evolve_tiled(st, pr, 1, 2, exact);
-        else run_resident(st, pr, c.second, 1, 2, exact, false, resident_mode(c.first));
+        if (c.strategy == QPE_STRATEGY_TILED) evolve_tiled(st, pr, 1, 2, exact);
+        else run_resident(st, pr, c.K, 1, 2, exact, false, resident_mode(c.strategy), c.replicas);
+        if (c.replicas > 1) check_device_error(st->ctx);
       };
       try {
         run();  // warm-up of this configuration
@@ -577,8 +603,9 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
       }
       if (ms < best) {
         best = ms;
-        strategy = c.first;
-        K = c.second;
+        strategy = c.strategy;
+        K = c.K;
+        replicas = c.replicas;
       }
     }
     if (best == 1e30f) strategy = QPE_STRATEGY_TILED;
@@ -589,6 +616,7 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
   st->tuned_exact = exact;
   st->tuned_strategy = strategy;
   st->tuned_cluster = K;
+  st->tuned_replicas = replicas;
 }
 
 static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts) {
@@ -615,15 +643,17 @@ static void evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* 
   st->probs_valid = false;
   if (first == last) return;
   const bool exact = st->dtype == QPE_C128 && !(opts && (opts->flags & QPE_EVOLVE_FP64_CONTRACT));
-  uint32_t strategy = 0, K = 0;
-  choose_strategy(st, pr, opts, exact, strategy, K);
+  uint32_t strategy = 0, K = 0, replicas = 1;
+  choose_strategy(st, pr, opts, exact, strategy, K, replicas);
   st->last_strategy = strategy;
   st->last_cluster = strategy == QPE_STRATEGY_TILED ? 0 : K;
+  st->last_replicas = replicas;
   if (strategy == QPE_STRATEGY_TILED) {
     evolve_tiled(st, pr, first, last, exact, in_place);
   } else {
-    run_resident(st, pr, K, first, last, exact, in_place, resident_mode(strategy));
+    run_resident(st, pr, K, first, last, exact, in_place, resident_mode(strategy), replicas);
     QPE_CK(cudaStreamSynchronize(st->ctx->stream));
+    if (replicas > 1) check_device_error(st->ctx);
   }
 }
 
@@ -1129,6 +1159,8 @@ int qpe_evolve(qpe_state* st, const qpe_program* pr, const qpe_evolve_opts* opts
     if (opts && opts->strategy > QPE_STRATEGY_LEAN_UNITS) throw Error(QPE_ERR_INVALID, "unknown strategy");
     if (opts && opts->cluster_size && (opts->cluster_size > 16 || (opts->cluster_size & (opts->cluster_size - 1))))
       throw Error(QPE_ERR_INVALID, "cluster_size must be a power of two <= 16");
+    if (opts && opts->replicas > 1 && opts->strategy != QPE_STRATEGY_LEAN_UNITS)
+      throw Error(QPE_ERR_INVALID, "replicas need QPE_STRATEGY_LEAN_UNITS");
     if (opts && (opts->flags & ~(QPE_EVOLVE_FP64_CONTRACT | QPE_EVOLVE_IN_PLACE)))
       throw Error(QPE_ERR_INVALID, "unknown evolve flag");
     evolve(st, pr, opts);
@@ -1153,6 +1185,12 @@ int qpe_state_phase_probs(qpe_state* st, double* probs) {
     QPE_CK(cudaStreamSynchronize(st->ctx->stream));
     check_device_error(st->ctx);
   });
+}
+
+int qpe_state_last_replicas(const qpe_state* st, uint32_t* replicas) {
+  if (!st || !replicas) return fail(QPE_ERR_INVALID, "null argument");
+  *replicas = st->last_replicas;
+  return QPE_OK;
 }
 
 int qpe_state_last_strategy(const qpe_state* st, uint32_t* strategy, uint32_t* cluster_size) {

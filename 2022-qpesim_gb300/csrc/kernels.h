@@ -125,7 +125,19 @@ struct ResidentInstance {
   const uint32_t* mix_words;
   const uint32_t* mix_slot;
   uint32_t mix_wp_words;
+  // Replicas (k_resident_lean, cluster > 1): `replicas` clusters each hold the
+  // whole block. Row and column passes are split between them (rows, columns by
+  // index modulo replicas) and every cluster takes the others' results through
+  // xbuf (two blocks, by exchange parity); xflag holds one exchange count per
+  // (replica, CTA), zero at launch. Column-pair passes run on every replica.
+  // replicas <= 1: one cluster. A wait for another replica that runs out ORs
+  // kResidentErrExchange into *err and the CTA stops waiting.
+  uint32_t replicas;
+  void* xbuf;
+  uint32_t* xflag;
+  int* err;
 };
+constexpr int kResidentErrExchange = 4;
 struct ResidentLaunch {
   const ResidentInstance* insts;  // device array, ninst entries
   uint32_t ninst;
@@ -141,6 +153,8 @@ struct ResidentLaunch {
                                   //    stage_elems is per group
   uint32_t meta_smem;             // 1: term descriptors, index pool, passes and line
                                   //    strings are staged in every CTA's shared memory
+  uint32_t replicas;              // clusters per instance (k_resident_lean; 0 or 1: one),
+                                  // launched cooperatively when more than one
   size_t smem_bytes;
 };
 // Upper bound of the resident kernels' static shared memory (a scratch element

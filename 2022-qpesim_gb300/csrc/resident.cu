@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(512) k_resident_group(const ResidentInstance* 
 // cluster's groups; rows are processed by the CTA that owns them.
 constexpr uint32_t kLeanWarps = 3;
 
-template <typename R, class A, bool MS>
+template <typename R, class A, bool MS, bool REP>
 __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* __restrict__ insts,
                                                        uint32_t stage_elems) {
   using C2 = typename Cx<R>::T;
@@ -463,7 +463,11 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
   cg::cluster_group cl = cg::this_cluster();
   const uint32_t K = cl.num_blocks();
   const uint32_t rank = cl.block_rank();
-  const ResidentInstance I = insts[blockIdx.x / K];
+  // Replica clusters (REP: the same number for every instance of a launch) and
+  // this cluster's replica, recomputed where needed rather than kept in registers.
+  auto nrep_f = [&]() { return REP && K > 1 ? max(__ldg(&insts[0].replicas), 1u) : 1u; };
+  auto rep_f = [&]() { return (blockIdx.x / K) % nrep_f(); };
+  const ResidentInstance I = insts[blockIdx.x / (K * nrep_f())];
   const uint32_t wpc = blockDim.x >> 5;
   const uint32_t gthreads = 32 * kLeanWarps, ngrp = wpc / kLeanWarps;
   const uint32_t grp = threadIdx.x / gthreads, gt = threadIdx.x - grp * gthreads;
@@ -517,6 +521,53 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
     for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) blk[i] = src[i];
   }
   barrier();
+
+  // Replica exchange after a row or column pass that the replicas split: this
+  // CTA publishes the amplitudes of its rows that its replica computed (element
+  // (a, b) belongs to replica b % nrep after a column pass, (a - row0) % nrep
+  // after a row pass) into buffer g % 2 for exchange g, raises its exchange
+  // count to g, waits (bounded) until the same CTA of every other replica has
+  // done so, and takes their amplitudes. Two buffers suffice: a replica writes
+  // exchange g + 2 only after the others' counts reached g + 1, which each
+  // raises after its reads of exchange g. Once a wait runs out
+  // (kResidentErrExchange ORed into *err) the CTA stops waiting. The exchange
+  // count and that state live in shared memory.
+  __shared__ uint32_t xstate;  // exchanges done << 1 | a wait ran out
+  if (threadIdx.x == 0) xstate = 0;
+  auto exchange = [&](bool col) {
+    const uint32_t nrep = nrep_f(), rep = rep_f();
+    const uint32_t xs = xstate, xgen = (xs >> 1) + 1;
+    C2* const xb = reinterpret_cast<C2*>(I.xbuf) + (size_t)(xgen & 1u) * ld + (size_t)row0 * Cb;
+    auto owner = [&](uint32_t i) { return (col ? i % Cb : i / Cb) % nrep; };
+    for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x)
+      if (owner(i) == rep) xb[i] = blk[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(I.xflag + rep * K + rank), "r"(xgen) : "memory");
+    }
+    bool late = false;
+    if (threadIdx.x < nrep && threadIdx.x != rep && !(xs & 1u)) {
+      const uint32_t* f = I.xflag + threadIdx.x * K + rank;
+      for (uint32_t it = 0;; ++it) {
+        uint32_t v;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
+        if (v >= xgen) break;
+        if (it == (1u << 20)) {
+          late = true;
+          break;
+        }
+        __nanosleep(128);
+      }
+    }
+    const bool failed = __syncthreads_or(late) || (xs & 1u);
+    if (threadIdx.x == 0) {
+      if (late) atomicOr(I.err, kResidentErrExchange);
+      xstate = (xgen << 1) | (failed ? 1u : 0u);
+    }
+    for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x)
+      if (owner(i) != rep) blk[i] = __ldcg(xb + i);
+  };
 
   const uint32_t nsweeps = I.steps * I.order;
   // per pass: kMixNoSchedule, or its window's block of warp programs (bits 0-19)
@@ -602,14 +653,16 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
             if (lane < nel) *gp = *sp;
           }
         } else if (P.type == PASS_ROW) {
-          // this CTA's rows, one per group tile, in place
-          for (uint32_t r = row0 + grp; r < row1; r += ngrp) {
+          // this CTA's rows of this replica, one per group tile, in place
+          const uint32_t nrep = nrep_f();
+          for (uint32_t r = row0 + rep_f() + nrep * grp; r < row1; r += nrep * ngrp) {
             C2* line = blk + (size_t)(r - row0) * Cb;
             group_line_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Cb, ldm<G>(strA + r), gt, gthreads,
                                     [&](uint32_t e) -> C2& { return line[e]; }, gbar, scratch);
           }
         } else if (P.type == PASS_COL) {
-          for (uint32_t b = grp * K + rank; b < Cb; b += K * ngrp) {
+          const uint32_t nrep = nrep_f();
+          for (uint32_t b = rep_f() + nrep * (grp * K + rank); b < Cb; b += nrep * K * ngrp) {
             const uint32_t lstr = ldm<G>(strB + b);
             if (K == 1) {
               group_line_ops<R, A, G>(ops, I.coef, pool, P.op0, P.op1, rev, Ca, lstr, gt, gthreads,
@@ -656,11 +709,17 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
         }
         if (in_group) wp_fetch(next_pi);
         barrier();
+        if (P.type != PASS_MIX && nrep_f() > 1) {
+          exchange(P.type == PASS_COL);
+          barrier();
+        }
         pj += span - 1;
       }
     }
-    C2* dst = gstate + (uint64_t)(I.in_place ? I.first : k) * ld + (uint64_t)row0 * Cb;
-    for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) dst[i] = blk[i];
+    if (rep_f() == 0) {
+      C2* dst = gstate + (uint64_t)(I.in_place ? I.first : k) * ld + (uint64_t)row0 * Cb;
+      for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x) dst[i] = blk[i];
+    }
     barrier();
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
@@ -668,21 +727,27 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
 
 template <typename R, class A, bool MS>
 static cudaError_t launch_res(const ResidentLaunch& rl, cudaStream_t s) {
+  const uint32_t nrep = rl.group == 3 && rl.cluster > 1 && rl.replicas > 1 ? rl.replicas : 1u;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(rl.ninst * rl.cluster);
+  cfg.gridDim = dim3(rl.ninst * nrep * rl.cluster);
   cfg.blockDim = dim3(32 * rl.warps_per_cta);
   cfg.dynamicSmemBytes = rl.smem_bytes;
   cfg.stream = s;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = rl.cluster;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
+  // replicas wait on one another: they must all be resident at once
+  at[1].id = cudaLaunchAttributeCooperative;
+  at[1].val.cooperative = 1;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = nrep > 1 ? 2 : 1;
   auto kern = rl.group == 1 ? k_resident_group<R, A, MS>
                             : (rl.group == 2 ? k_resident<R, A, MS, true>
-                                             : (rl.group == 3 ? k_resident_lean<R, A, MS> : k_resident<R, A, MS, false>));
+                                             : (rl.group == 3 ? (nrep > 1 ? k_resident_lean<R, A, MS, true>
+                                                                          : k_resident_lean<R, A, MS, false>)
+                                                              : k_resident<R, A, MS, false>));
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rl.smem_bytes);
   if (e) return e;
   if (rl.cluster > 8) {
@@ -712,7 +777,9 @@ static cudaError_t carveout_t(int percent) {
   if (e) return e;
   e = cudaFuncSetAttribute(k_resident<R, A, MS, true>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
   if (e) return e;
-  e = cudaFuncSetAttribute(k_resident_lean<R, A, MS>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+  e = cudaFuncSetAttribute(k_resident_lean<R, A, MS, false>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+  if (e) return e;
+  e = cudaFuncSetAttribute(k_resident_lean<R, A, MS, true>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
   if (e) return e;
   return cudaFuncSetAttribute(k_resident_group<R, A, MS>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
 }

@@ -146,7 +146,7 @@ class DeviceState:
         N.check(self._lib.qpe_state_zero(self._h))
 
     def evolve(self, program: Program, first_power: int = 0, last_power: int = 0, strategy: int = 0,
-               cluster_size: int = 0, fp64_contract: bool = False) -> None:
+               cluster_size: int = 0, fp64_contract: bool = False, replicas: int = 0) -> None:
         """strategy: 0 auto (autotuned per program), 1 one CTA resident in shared
         memory, 2 a cluster of cluster_size CTAs (0: smallest that fits), 3
         global-memory tile passes, 4 a cluster whose tiles are processed by
@@ -154,18 +154,20 @@ class DeviceState:
         whose column-pair tiles are processed as in 4 and row and column tiles
         as in 2, 6 a cluster whose rows, columns and column pairs are each
         processed by a three-warp group (pair updates over four lanes, diagonal
-        updates over two). fp64_contract allows FMAs in complex128 (within 1e-12 of the
-        reference instead of bit-identical)."""
+        updates over two), 7 as 6 with the column-pair passes as windows of
+        independent update units; with 7, `replicas` clusters (up to 4) each hold
+        the block and split the row and column passes. fp64_contract allows FMAs
+        in complex128 (within 1e-12 of the reference instead of bit-identical)."""
         opts = N.EvolveOpts(strategy, first_power, last_power, cluster_size,
-                            N.QPE_EVOLVE_FP64_CONTRACT if fp64_contract else 0, 0)
+                            N.QPE_EVOLVE_FP64_CONTRACT if fp64_contract else 0, 0, replicas)
         N.check(self._lib.qpe_evolve(self._h, program._h, C.byref(opts)))
 
     def evolve_in_place(self, program: Program, block: int = 1, repeats: int = 1, strategy: int = 0,
-                        cluster_size: int = 0, fp64_contract: bool = False) -> None:
+                        cluster_size: int = 0, fp64_contract: bool = False, replicas: int = 0) -> None:
         """Applies the program's power `repeats` times to block `block` in place
         (time_evolve_iqpe's evolution with block = 1)."""
         flags = N.QPE_EVOLVE_IN_PLACE | (N.QPE_EVOLVE_FP64_CONTRACT if fp64_contract else 0)
-        opts = N.EvolveOpts(strategy, block, 0, cluster_size, flags, repeats)
+        opts = N.EvolveOpts(strategy, block, 0, cluster_size, flags, repeats, replicas)
         N.check(self._lib.qpe_evolve(self._h, program._h, C.byref(opts)))
 
     def qift(self) -> None:
@@ -175,6 +177,12 @@ class DeviceState:
         p = np.zeros(1 << self.precision)
         N.check(self._lib.qpe_state_phase_probs(self._h, p.ctypes.data_as(C.POINTER(C.c_double))))
         return p
+
+    def last_replicas(self) -> int:
+        """Replica clusters of the last evolve (1 unless strategy 7 ran with replicas)."""
+        r = C.c_uint32()
+        N.check(self._lib.qpe_state_last_replicas(self._h, C.byref(r)))
+        return r.value
 
     def last_strategy(self) -> tuple:
         """(strategy, cluster size) of the last evolve: 1 resident, 2 cluster, 3 tiled, 4 grouped cluster,

@@ -96,9 +96,11 @@ DEFAULT_WORKLOAD = "plain-n16"
 # DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum) from the ncu captures summarised under profiles/.
 MEASURED_TRAFFIC = {
-    "plain-n16": (338_944, "k_resident_lean, cluster of 16: one launch runs every power; the capture of a "
-                           "2-power launch read the block and the program once (0.34 MB) and wrote nothing back to "
-                           "DRAM, the snapshots staying in L2 (ncu capture of the same kernel, small case)"),
+    "plain-n16": (25_823_744, "k_resident_lean with update-unit windows, cluster of 16: one launch runs every "
+                              "power; the capture of a 2-power launch read the block, the program and the warp "
+                              "programs of the column-pair windows once (25.8 MB, then L2-resident) and wrote "
+                              "nothing back to DRAM, the snapshots staying in L2 (ncu capture of the same kernel, "
+                              "small case)"),
     "precision-n24": (3_810_000, "k_pass MIX launch, one tile per CTA, pass image in shared memory: DRAM reads "
                                  "of a cold-cache ncu capture at P = 3 (3.79-3.82 MB; the 6.8 MB working block is "
                                  "the same at any P, and a MIX pass touches its column pairs, about half of it)"),
@@ -413,14 +415,17 @@ def run_ours(args, w, rank, ws, local):
         kernel = "k_pass (evolution tile passes, one launch per pass)"
         launches = args.steps * (npow * (info["num_passes_per_power"] + 2) + 1 + 2 + 1)
     else:
-        kname = {4: "k_resident_group", 6: "k_resident_lean"}.get(strat, "k_resident")
-        kernel = (f"{kname} (whole evolution in one launch, "
-                  f"cluster of {kc} CTA(s){', column pairs by four-warp groups' if strat == 5 else ''})")
+        kname = {4: "k_resident_group", 6: "k_resident_lean", 7: "k_resident_lean"}.get(strat, "k_resident")
+        extra = {5: ", column pairs by four-warp groups",
+                 7: ", column-pair passes as windows of independent update units"}.get(strat, "")
+        kernel = f"{kname} (whole evolution in one launch, cluster of {kc} CTA(s){extra})"
         launches = args.steps * (1 + 2)
     strategy_name = {1: "resident (one CTA)", 2: f"cluster of {kc} CTAs", 3: "tiled passes",
                      4: f"cluster of {kc} CTAs, four-warp tile groups",
                      5: f"cluster of {kc} CTAs, column-pair tiles by four-warp groups",
-                     6: f"cluster of {kc} CTAs, every tile by a three-warp group"}.get(strat, "?")
+                     6: f"cluster of {kc} CTAs, every tile by a three-warp group",
+                     7: f"cluster of {kc} CTAs, three-warp groups, column-pair passes as windows of "
+                        f"independent update units"}.get(strat, "?")
     line = {
         "metric": "amplitude-term updates/s per Trotter step",
         "value": value,
@@ -437,7 +442,7 @@ def run_ours(args, w, rank, ws, local):
         "config": workload_config(args, w, prog.touches_per_power, ws),
         "kernel_strategy": strategy_name,
         "roofline": roofline_single(w, achieved, peak, peak_kind, kernel, touches_step, ev_s, fp64_peak,
-                                    cluster_sms=kc if strat in (2, 4, 5, 6) else (1 if strat == 1 else 0)),
+                                    cluster_sms=kc if strat in (2, 4, 5, 6, 7) else (1 if strat == 1 else 0)),
         "e2e": {"value": e2e_value, "unit": "touches/s",
                 "h2d_bytes_per_step": int(st.ld * dtype().itemsize),
                 "d2h_bytes_per_step": int(st.size * dtype().itemsize + (1 << P) * 8)},
@@ -969,7 +974,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--strategy", type=int, default=0,
                     help="0 auto, 1 one-CTA resident, 2 cluster, 3 tiled, 4 cluster with four-warp groups, "
-                         "5 cluster with column pairs by four-warp groups, 6 cluster of three-warp groups")
+                         "5 cluster with column pairs by four-warp groups, 6 cluster of three-warp groups, "
+                         "7 as 6 with column-pair passes as windows of update units")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per cluster for --strategy 2 (0: smallest)")
     ap.add_argument("--powers", type=int, default=0,
                     help="evolve only the first K controlled powers (profiling runs; not a workload's figure)")

@@ -258,6 +258,10 @@ typedef struct qpe_evolve_opts {
   uint32_t cluster_size; /* QPE_STRATEGY_CLUSTER: CTAs per cluster (0 = auto) */
   uint32_t flags;        /* QPE_EVOLVE_* */
   uint32_t repeats;      /* QPE_EVOLVE_IN_PLACE: applications of the power (0 = 1) */
+  uint32_t replicas;     /* QPE_STRATEGY_LEAN_UNITS: clusters that each hold the whole block
+                            and split the row and column passes between them, exchanging
+                            their results through global memory (0 or 1: one cluster; at
+                            most 4; launched cooperatively). The autotuner tries 1 to 3. */
 } qpe_evolve_opts;
 
 /* block_k <- U * block_{k-1} for k = 1 .. 2^P - 1 on the device (opts may be NULL). */
@@ -270,6 +274,8 @@ int qpe_state_phase_probs(qpe_state* st, double* probs);
 int qpe_state_block_norms(qpe_state* st, double* norms);
 /* Strategy (QPE_STRATEGY_*) and cluster size the last qpe_evolve on this state ran. */
 int qpe_state_last_strategy(const qpe_state* st, uint32_t* strategy, uint32_t* cluster_size);
+/* Replica clusters (qpe_evolve_opts::replicas) the last qpe_evolve on this state ran. */
+int qpe_state_last_replicas(const qpe_state* st, uint32_t* replicas);
 
 /* ---- batching form ----------------------------------------------------------------
  * Many Hamiltonians (programs) evolved, transformed and read out by one launch of

@@ -246,13 +246,16 @@ def test_strategies_bit_identical(gpu, orc, strategy, cluster, n, na, nb, P):
     assert np.array_equal(st.download(), ref)
 
 
-@pytest.mark.parametrize("strategy,cluster", [(0, 0), (6, 16), (6, 8), (7, 16), (7, 8), (3, 0)])
-def test_headline_configuration(gpu, orc, strategy, cluster):
+@pytest.mark.parametrize("strategy,cluster,replicas", [(0, 0, 0), (6, 16, 0), (6, 8, 0), (7, 16, 0), (7, 8, 0),
+                                                       (7, 16, 2), (7, 16, 3), (7, 8, 2), (3, 0, 0)])
+def test_headline_configuration(gpu, orc, strategy, cluster, replicas):
     """The plain-n16 bench workload exactly as it is timed, at P = 3: n = 16,
     N = 8, seed-0 integrals, 2nd-order Trotter (forward and reversed sweeps at
     dt / 2 = 0.025), 4 steps per power, Hartree-Fock start, complex128. Autotuned
     (the strategy the bench ends up with) and forced to the three-warp-group
-    cluster of 16 and 8 CTAs and to the tile passes: the register is bit-identical
+    cluster of 16 and 8 CTAs (with the column-pair passes as tiles and as update
+    units, and with 2 or 3 replica clusters splitting the row and column passes)
+    and to the tile passes: the register is bit-identical
     to the oracle's order-2, 4-step evolution, and after the QIFT the register too,
     and the histogram within 1e-12."""
     q = gpu
@@ -265,9 +268,10 @@ def test_headline_configuration(gpu, orc, strategy, cluster):
     st = q.DeviceState(M, e, e, P)
     b0 = q.hf_block0(st.c_alpha, st.c_beta, P)
     st.upload(b0)
-    st.evolve(prog, strategy=strategy, cluster_size=cluster)
+    st.evolve(prog, strategy=strategy, cluster_size=cluster, replicas=replicas)
     if strategy in (6, 7):
         assert st.last_strategy() == (strategy, cluster)
+        assert st.last_replicas() == max(replicas, 1)
     if strategy == 7:
         # every one of the 392 column-pair passes of a sweep as update units
         assert prog.unit_schedule() == (cluster, 392)
