@@ -425,7 +425,7 @@ static bool plan_resident(const qpe_program* pr, const qpe_state* st, uint32_t K
 // Most consecutive column-pair passes one window of update units may take.
 constexpr uint32_t kMixWindowPasses = 8;
 // Replica clusters a lean launch may have (QPE_STRATEGY_LEAN_UNITS).
-constexpr uint32_t kMaxReplicas = 4;
+constexpr uint32_t kMaxReplicas = 8;
 
 // The column-pair update-unit schedule of `pr` for cluster K, wpc warps per CTA
 // and group stages of `stage` elements, built from the device's index pool on
@@ -466,7 +466,7 @@ static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint3
   if (replicas > 1) {
     // replica clusters of the lean kernel, each holding the whole block
     if (rl.group != 3 || K < 2) throw Error(QPE_ERR_INVALID, "replicas need a three-warp-group cluster of 2 or more");
-    if (replicas > kMaxReplicas) throw Error(QPE_ERR_INVALID, "at most 4 replicas");
+    if (replicas > kMaxReplicas) throw Error(QPE_ERR_INVALID, "at most 8 replicas");
     if (st->xbuf.bytes < 2 * st->ld * st->esz) st->xbuf.alloc(2 * st->ld * st->esz);
     if (!st->xflag.p) st->xflag.alloc(16 * kMaxReplicas * sizeof(uint32_t));
     QPE_CK(cudaMemsetAsync(st->xflag.p, 0, st->xflag.bytes, st->ctx->stream));
@@ -570,7 +570,7 @@ static void choose_strategy(qpe_state* st, const qpe_program* pr, const qpe_evol
     if (plan_resident(pr, st, c, rl, ri, 2)) cands.push_back({(uint32_t)QPE_STRATEGY_HYBRID, c, one});
     if (plan_resident(pr, st, c, rl, ri, 3)) cands.push_back({(uint32_t)QPE_STRATEGY_LEAN, c, one});
     if (plan_resident(pr, st, c, rl, ri, 4) && ensure_mix_units(pr, c, rl.warps_per_cta, rl.stage_elems))
-      for (uint32_t r = 1; r <= (c >= 8 ? 3u : 1u); ++r) cands.push_back({(uint32_t)QPE_STRATEGY_LEAN_UNITS, c, r});
+      for (uint32_t r = 1; r <= (c >= 8 ? 5u : 1u); ++r) cands.push_back({(uint32_t)QPE_STRATEGY_LEAN_UNITS, c, r});
   }
   cands.push_back({(uint32_t)QPE_STRATEGY_TILED, 0u, 1u});
   if (cands.size() == 1) {

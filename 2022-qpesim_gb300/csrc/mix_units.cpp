@@ -159,30 +159,52 @@ bool place_window(const HostProgram& hp, const std::vector<Comp>& comps, uint32_
     }
   }
   teams.insert(teams.end(), packs.begin(), packs.end());
-  // CTA with the least quads per level that has room: a whole free group for a
-  // team of two or three warps, a free warp for one; stage room in that group.
-  std::vector<uint32_t> load(K, 0), gwarps((size_t)K * groups, 0), gstage((size_t)K * groups, 0);
+  // Place each team where it adds least to the most warps on one SM
+  // sub-partition of a CTA (warp w runs on sub-partition w % 4; an FP64
+  // instruction holds its sub-partition's unit for about 62 cycles, so two warps
+  // there double a level's FP64 time), then where the CTA has the fewest update
+  // slots per level. A team of two or three warps takes warps 0 .. tw - 1 of an
+  // empty group (it synchronises by the group's named barrier); a single warp
+  // any free warp of a group; the group's stage must have room for its amplitudes.
+  std::vector<uint32_t> load(K, 0), gmask((size_t)K * groups, 0), gstage((size_t)K * groups, 0);
+  std::vector<uint32_t> sub((size_t)K * 4, 0);
   std::fill(block, block + (size_t)K * wpc * wp_words, 0u);
   const uint32_t Cb = (uint32_t)hp.Cb;
   for (const Team& tm : teams) {
-    int best_cta = -1, best_grp = -1;
-    for (uint32_t r = 0; r < K; ++r) {
-      if (best_cta >= 0 && load[r] >= load[best_cta]) continue;
+    int best_cta = -1;
+    uint32_t best_w0 = 0, best_score0 = ~0u, best_score1 = ~0u;
+    for (uint32_t r = 0; r < K; ++r)
       for (uint32_t g = 0; g < groups; ++g) {
         const size_t gi = (size_t)r * groups + g;
-        const bool room = tm.tw > 1 ? gwarps[gi] == 0 : gwarps[gi] < kMaxTeam;
-        if (room && gstage[gi] + tm.elems <= stage_elems) {
-          best_cta = (int)r;
-          best_grp = (int)g;
-          break;
+        if (gstage[gi] + tm.elems > stage_elems) continue;
+        for (uint32_t i = 0; i < (tm.tw > 1 ? 1u : kMaxTeam); ++i) {
+          const uint32_t bits = tm.tw > 1 ? (1u << tm.tw) - 1 : 1u << i;
+          if (gmask[gi] & (tm.tw > 1 ? 7u : bits)) continue;
+          uint32_t worst = 0;
+          for (uint32_t s4 = 0; s4 < 4; ++s4) {
+            uint32_t c = sub[(size_t)r * 4 + s4];
+            for (uint32_t w = 0; w < kMaxTeam; ++w)
+              if ((bits >> w & 1u) && (g * kMaxTeam + w) % 4 == s4) ++c;
+            worst = std::max(worst, c);
+          }
+          const uint32_t score1 = load[r] + tm.quads;
+          if (worst < best_score0 || (worst == best_score0 && score1 < best_score1)) {
+            best_score0 = worst;
+            best_score1 = score1;
+            best_cta = (int)r;
+            best_w0 = g * kMaxTeam + (tm.tw > 1 ? 0u : i);
+          }
         }
       }
-    }
     if (best_cta < 0) return false;
-    const size_t gi = (size_t)best_cta * groups + best_grp;
-    const uint32_t w0 = (uint32_t)best_grp * kMaxTeam + gwarps[gi];
+    const uint32_t g = best_w0 / kMaxTeam;
+    const size_t gi = (size_t)best_cta * groups + g;
+    const uint32_t w0 = best_w0;
     const uint32_t ebase = gstage[gi];
-    gwarps[gi] += tm.tw;
+    for (uint32_t w = 0; w < tm.tw; ++w) {
+      gmask[gi] |= 1u << (w0 + w - g * kMaxTeam);
+      ++sub[(size_t)best_cta * 4 + (w0 + w) % 4];
+    }
     gstage[gi] += tm.elems;
     load[best_cta] += tm.quads;
     if (ebase + tm.elems > kIdxLimit) return false;

@@ -155,7 +155,7 @@ class DeviceState:
         as in 2, 6 a cluster whose rows, columns and column pairs are each
         processed by a three-warp group (pair updates over four lanes, diagonal
         updates over two), 7 as 6 with the column-pair passes as windows of
-        independent update units; with 7, `replicas` clusters (up to 4) each hold
+        independent update units; with 7, `replicas` clusters (up to 8) each hold
         the block and split the row and column passes. fp64_contract allows FMAs
         in complex128 (within 1e-12 of the reference instead of bit-identical)."""
         opts = N.EvolveOpts(strategy, first_power, last_power, cluster_size,

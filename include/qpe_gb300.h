@@ -261,7 +261,7 @@ typedef struct qpe_evolve_opts {
   uint32_t replicas;     /* QPE_STRATEGY_LEAN_UNITS: clusters that each hold the whole block
                             and split the row and column passes between them, exchanging
                             their results through global memory (0 or 1: one cluster; at
-                            most 4; launched cooperatively). The autotuner tries 1 to 3. */
+                            most 8; launched cooperatively). The autotuner tries 1 to 5. */
 } qpe_evolve_opts;
 
 /* block_k <- U * block_{k-1} for k = 1 .. 2^P - 1 on the device (opts may be NULL). */

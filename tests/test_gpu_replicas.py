@@ -1,5 +1,5 @@
 """Replica clusters of the lean resident kernel (strategy 7 with replicas > 1):
-2 to 4 thread-block clusters each hold the whole block, split every row and
+2 to 8 thread-block clusters each hold the whole block, split every row and
 column pass between them and exchange their results through global memory
 (bounded waits, cooperative launch); column-pair passes run on every replica.
 The register must be the oracle's bit for bit, as with one cluster."""
@@ -63,4 +63,4 @@ def test_replicas_rejected_outside_strategy_7(gpu):
     with pytest.raises(q.QpeError):
         st.evolve(prog, strategy=6, cluster_size=2, replicas=2)
     with pytest.raises(q.QpeError):
-        st.evolve(prog, strategy=7, cluster_size=2, replicas=5)
+        st.evolve(prog, strategy=7, cluster_size=2, replicas=9)
