@@ -410,6 +410,7 @@ def run_ours(args, w, rank, ws, local):
     peak, peak_kind = peaks()
     info = prog.info
     strat, kc = st.last_strategy()
+    nrep = st.last_replicas()
     fp64_peak = measure_fp64_peak(N, ctx) if w["dtype"] == "c128" else None
     if strat == 3:
         kernel = "k_pass (evolution tile passes, one launch per pass)"
@@ -418,6 +419,8 @@ def run_ours(args, w, rank, ws, local):
         kname = {4: "k_resident_group", 6: "k_resident_lean", 7: "k_resident_lean"}.get(strat, "k_resident")
         extra = {5: ", column pairs by four-warp groups",
                  7: ", column-pair passes as windows of independent update units"}.get(strat, "")
+        if nrep > 1:
+            extra += f", {nrep} replica clusters splitting the row and column passes"
         kernel = f"{kname} (whole evolution in one launch, cluster of {kc} CTA(s){extra})"
         launches = args.steps * (1 + 2)
     strategy_name = {1: "resident (one CTA)", 2: f"cluster of {kc} CTAs", 3: "tiled passes",
@@ -425,7 +428,7 @@ def run_ours(args, w, rank, ws, local):
                      5: f"cluster of {kc} CTAs, column-pair tiles by four-warp groups",
                      6: f"cluster of {kc} CTAs, every tile by a three-warp group",
                      7: f"cluster of {kc} CTAs, three-warp groups, column-pair passes as windows of "
-                        f"independent update units"}.get(strat, "?")
+                        f"independent update units" + (f", {nrep} replica clusters" if nrep > 1 else "")}.get(strat, "?")
     line = {
         "metric": "amplitude-term updates/s per Trotter step",
         "value": value,
@@ -442,7 +445,7 @@ def run_ours(args, w, rank, ws, local):
         "config": workload_config(args, w, prog.touches_per_power, ws),
         "kernel_strategy": strategy_name,
         "roofline": roofline_single(w, achieved, peak, peak_kind, kernel, touches_step, ev_s, fp64_peak,
-                                    cluster_sms=kc if strat in (2, 4, 5, 6, 7) else (1 if strat == 1 else 0)),
+                                    cluster_sms=kc * nrep if strat in (2, 4, 5, 6, 7) else (1 if strat == 1 else 0)),
         "e2e": {"value": e2e_value, "unit": "touches/s",
                 "h2d_bytes_per_step": int(st.ld * dtype().itemsize),
                 "d2h_bytes_per_step": int(st.size * dtype().itemsize + (1 << P) * 8)},
