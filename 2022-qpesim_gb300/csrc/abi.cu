@@ -330,7 +330,9 @@ static bool plan_resident_lean(const qpe_program* pr, const qpe_state* st, uint3
   const uint64_t Rk = (Ca + K - 1) / K;
   const size_t meta = resident_meta_bytes((uint32_t)hp.ops.size(), (uint32_t)hp.pool_words,
                                           (uint32_t)hp.passes.size(), (uint32_t)Ca, (uint32_t)Cb);
-  const uint64_t stage = K > 1 ? 2 * Ca : 0;
+  // a group's stage holds one column pair, or with units the amplitudes of its
+  // three warps' programs (up to kMixWarpAmps each)
+  const uint64_t stage = K > 1 ? std::max<uint64_t>(2 * Ca, units ? 3 * kMixWarpAmps : 0) : 0;
   if (units && K < 2) return false;
   const size_t wp_bytes = units ? (size_t)mix_wp_words(hp) * 4 : 0;
   for (int with_meta = 1; with_meta >= 0; --with_meta)

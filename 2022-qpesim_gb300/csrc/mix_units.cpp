@@ -10,7 +10,7 @@ namespace qpe {
 namespace {
 
 constexpr uint32_t kQuads = 8;         // quads of lanes per warp
-constexpr uint32_t kLanes = 32;        // amplitudes a warp gathers (one per lane)
+constexpr uint32_t kLanes = kMixWarpAmps;  // amplitudes a warp gathers (two per lane)
 constexpr uint32_t kMaxTeam = 3;       // warps of a three-warp group
 constexpr uint32_t kIdxLimit = 1024;   // stage indices are 10-bit
 constexpr uint32_t kLineLimit = 2048;  // rows and columns are 11-bit
@@ -32,7 +32,8 @@ struct Comp {
 struct Team {
   uint32_t tw = 1;
   std::vector<uint32_t> units;
-  uint32_t quads = 0, elems = 0;
+  uint32_t quads = 0, elems = 0;  // most update slots at one level, amplitudes
+  std::vector<uint32_t> used;     // update slots per level (packs of small units)
 };
 
 struct UnionFind {
@@ -136,26 +137,40 @@ bool place_window(const HostProgram& hp, const std::vector<Comp>& comps, uint32_
     teams.push_back(tm);
   }
   std::stable_sort(teams.begin(), teams.end(), [](const Team& a, const Team& b) { return a.quads > b.quads; });
-  std::stable_sort(small.begin(), small.end(),
-                   [&](uint32_t a, uint32_t b) { return comps[a].maxper > comps[b].maxper; });
+  auto total = [&](uint32_t c) {
+    size_t t = 0;
+    for (const auto& l : comps[c].lev) t += l.size();
+    return t;
+  };
+  std::stable_sort(small.begin(), small.end(), [&](uint32_t a, uint32_t b) { return total(a) > total(b); });
+  // A warp's quads are reassigned at every level, so small units share a warp
+  // as long as their updates at each level fit its 8 quads (and their
+  // amplitudes its 32 lanes): fewer warps, and fewer FP64 instructions per level
+  // on each SM sub-partition.
   std::vector<Team> packs;
   for (uint32_t c : small) {
-    const uint32_t q = comps[c].maxper, e = (uint32_t)comps[c].nodes.size();
-    bool placed = false;
-    for (Team& pk : packs)
-      if (pk.quads + q <= kQuads && pk.elems + e <= kLanes) {
-        pk.units.push_back(c);
-        pk.quads += q;
-        pk.elems += e;
-        placed = true;
+    const Comp& cc = comps[c];
+    const uint32_t e = (uint32_t)cc.nodes.size();
+    Team* fit = nullptr;
+    for (Team& pk : packs) {
+      if (pk.elems + e > kLanes) continue;
+      bool ok = true;
+      for (uint32_t k = 0; k < levels && ok; ++k) ok = pk.used[k] + cc.lev[k].size() <= kQuads;
+      if (ok) {
+        fit = &pk;
         break;
       }
-    if (!placed) {
-      Team pk;
-      pk.units.push_back(c);
-      pk.quads = q;
-      pk.elems = e;
-      packs.push_back(pk);
+    }
+    if (!fit) {
+      packs.emplace_back();
+      fit = &packs.back();
+      fit->used.assign(levels, 0);
+    }
+    fit->units.push_back(c);
+    fit->elems += e;
+    for (uint32_t k = 0; k < levels; ++k) {
+      fit->used[k] += (uint32_t)cc.lev[k].size();
+      fit->quads = std::max(fit->quads, fit->used[k]);
     }
   }
   teams.insert(teams.end(), packs.begin(), packs.end());
@@ -214,27 +229,27 @@ bool place_window(const HostProgram& hp, const std::vector<Comp>& comps, uint32_
     uint32_t* wp[kMaxTeam];
     for (uint32_t w = 0; w < tm.tw; ++w) {
       wp[w] = block + ((size_t)best_cta * wpc + w0 + w) * wp_words;
-      wp[w][0] = (tm.tw << 6) | (levels << 8);
+      wp[w][0] = (tm.tw << 7) | (levels << 9);
       wp[w][1] = op0;
     }
-    uint32_t e0 = 0, q0 = 0;
+    uint32_t e0 = 0;
+    std::vector<uint32_t> q0(levels, 0);  // update slots taken at each level
     for (uint32_t ci : tm.units) {
       const Comp& c = comps[ci];
       for (uint32_t i = 0; i < c.nodes.size(); ++i) {
         const uint32_t row = c.nodes[i] / Cb, col = c.nodes[i] % Cb, e = e0 + i;
         uint32_t* w = wp[e / kLanes];
         w[kMixWpHeader + e % kLanes] = row | (col << 11) | ((ebase + e) << 22);
-        w[0] = (w[0] & ~63u) | ((w[0] & 63u) + 1);
+        w[0] = (w[0] & ~127u) | ((w[0] & 127u) + 1);
       }
       for (uint32_t k = 0; k < levels; ++k)
         for (uint32_t j = 0; j < c.lev[k].size(); ++j) {
           const Upd& up = c.lev[k][j];
-          const uint32_t slot = q0 + j;
+          const uint32_t slot = q0[k]++;
           wp[slot / kQuads][kMixWpHeader + kLanes + kQuads * k + slot % kQuads] =
               (ebase + e0 + up.l) | ((ebase + e0 + up.r) << 10) | (up.par << 20) | (1u << 21);
         }
       e0 += (uint32_t)c.nodes.size();
-      q0 += c.maxper;
     }
   }
   return true;

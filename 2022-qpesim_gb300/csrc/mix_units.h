@@ -14,9 +14,10 @@
 // gather, one scatter and one cluster barrier instead of w of each.
 //
 // The host grows each window while its units still fit (at most 24 updates per
-// level and 96 amplitudes per unit; the kernel's warps and stages) and packs the
-// units into warp programs: small units share a warp (each on its own quads of
-// lanes and its own range of the group's stage), large ones take a team of two
+// level and 192 amplitudes per unit; the kernel's warps and stages) and packs the
+// units into warp programs: small units share a warp (their updates at each
+// level on its 8 quads of lanes, their amplitudes, up to 64, on its own range of
+// the group's stage), large ones take a team of two
 // or three warps of one three-warp group, which then synchronises by the group's
 // named barrier. Units go to the CTA with the least work per level.
 //
@@ -25,12 +26,12 @@
 // 20-27), the same for every pass of the window. A sweep meets a window at its
 // first pass (forward) or its last (reversed), runs it, and skips its other passes.
 //
-// Warp program (kMixWpHeader + 32 + 8 * levels words, a multiple of 4):
-//   w[0]                     nelem (bits 0-5, <= 32) | team warps (bits 6-7; 0: idle)
-//                            | levels (bits 8-15)
+// Warp program (kMixWpHeader + kMixWarpAmps + 8 * levels words, a multiple of 4):
+//   w[0]                     nelem (bits 0-6, <= 64) | team warps (bits 7-8; 0: idle)
+//                            | levels (bits 9-16)
 //   w[1]                     first term of the window (its op index)
-//   w[kMixWpHeader + l]      gather entry of lane l: row | col << 11 | stage index << 22
-//   w[kMixWpHeader + 32 + 8 k + u]
+//   w[kMixWpHeader + l]      gather entry l (lane l % 32): row | col << 11 | stage index << 22
+//   w[kMixWpHeader + kMixWarpAmps + 8 k + u]
 //                            update of quad u at level k: left stage index
 //                            | right stage index << 10 | parity << 20 | valid << 21
 #ifndef QPE_MIX_UNITS_H_

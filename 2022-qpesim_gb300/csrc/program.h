@@ -72,9 +72,11 @@ constexpr uint32_t kPairChunk = 4;
 constexpr uint32_t kPairTrips = 3;
 
 // Column-pair passes as update units (mix_units.h): words before a warp
-// program's gather entries, the most terms a scheduled window may have, and the
-// slot of a pass without a schedule.
+// program's gather entries, the amplitudes one warp gathers (two per lane), the
+// most terms a scheduled window may have, and the slot of a pass without a
+// schedule.
 constexpr uint32_t kMixWpHeader = 4;
+constexpr uint32_t kMixWarpAmps = 64;
 constexpr uint32_t kMixMaxLevels = 24;
 constexpr uint32_t kMixNoSchedule = 0xffffffffu;
 

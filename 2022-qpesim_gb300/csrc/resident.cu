@@ -613,18 +613,26 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
           asm volatile("cp.async.wait_all;" ::: "memory");
           __syncwarp();
           const uint32_t hdr = wp_s[0], op0 = wp_s[1];
-          const uint32_t tw = (hdr >> 6) & 3u;
+          const uint32_t tw = (hdr >> 7) & 3u;
           if (tw) {
             auto tsync = [&]() {
               if (tw == 1) __syncwarp();
               else asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(32 * tw) : "memory");
             };
             C2* const gst = blk + (size_t)Rk * Cb + (size_t)grp * stage_elems;
-            const uint32_t nel = hdr & 63u, nlev = (hdr >> 8) & 0xffu;
+            // up to two amplitudes per lane: entries lane and lane + 32
+            const uint32_t nel = hdr & 127u, nlev = (hdr >> 9) & 0xffu;
             const uint32_t gw = lane < nel ? wp_s[kMixWpHeader + lane] : 0u;
+            const uint32_t gw2 = lane + 32 < nel ? wp_s[kMixWpHeader + 32 + lane] : 0u;
             C2* const gp = at(gw & 2047u, (gw >> 11) & 2047u);
             C2* const sp = gst + (gw >> 22);
-            if (lane < nel) *sp = *gp;
+            C2* const gp2 = at(gw2 & 2047u, (gw2 >> 11) & 2047u);
+            C2* const sp2 = gst + (gw2 >> 22);
+            if (lane < nel) {
+              const C2 v = *gp;
+              if (lane + 32 < nel) *sp2 = *gp2;
+              *sp = v;
+            }
             tsync();
             const uint32_t q = lane & 3u, quad = lane >> 2;
             const bool side1 = q >= 2;
@@ -632,14 +640,14 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
             R* const gr = reinterpret_cast<R*>(gst);
             // the next level's update word and coefficients are loaded a level ahead
             uint32_t lv_n = rev ? nlev - 1 : 0;
-            uint32_t uw_n = wp_s[kMixWpHeader + 32 + 8 * lv_n + quad];
+            uint32_t uw_n = wp_s[kMixWpHeader + kMixWarpAmps + 8 * lv_n + quad];
             uint4 b_n = ldm<G>(reinterpret_cast<const uint4*>(ops + op0 + lv_n) + 1);
             for (uint32_t i = 0; i < nlev; ++i) {
               const uint32_t uw = uw_n;
               const uint4 b = b_n;
               if (i + 1 < nlev) {
                 lv_n = rev ? nlev - 2 - i : i + 1;
-                uw_n = wp_s[kMixWpHeader + 32 + 8 * lv_n + quad];
+                uw_n = wp_s[kMixWpHeader + kMixWarpAmps + 8 * lv_n + quad];
                 b_n = ldm<G>(reinterpret_cast<const uint4*>(ops + op0 + lv_n) + 1);
               }
               const R c = (R)__hiloint2double((int)b.y, (int)b.x), t = (R)__hiloint2double((int)b.w, (int)b.z);
@@ -651,6 +659,7 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
               tsync();
             }
             if (lane < nel) *gp = *sp;
+            if (lane + 32 < nel) *gp2 = *sp2;
           }
         } else if (P.type == PASS_ROW) {
           // this CTA's rows of this replica, one per group tile, in place

@@ -13,7 +13,7 @@
 //     (gather into per-group stages, level by level, scatter back),
 // and counts every difference between the two blocks (bit for bit) and every
 // broken invariant the kernel relies on: a team of two or three warps is warps
-// 0 .. tw - 1 of one group with equal headers; at most 32 amplitudes per warp;
+// 0 .. tw - 1 of one group with equal headers; at most 64 amplitudes per warp;
 // stage indices inside the group's stage and used by one team; rows and columns
 // inside the block; each amplitude gathered at most once per window; every
 // update inside its own team's amplitudes; the window's first term in w[1].
@@ -131,26 +131,26 @@ extern "C" int mix_units_check(unsigned M, unsigned na, unsigned nb, const qpe_t
     const uint32_t* blk = mu.words.data() + (size_t)slot * K * wpc * mu.wp_words;
     auto W = [&](uint32_t r, uint32_t w) { return blk + ((size_t)r * wpc + w) * mu.wp_words; };
     auto team_of = [&](uint32_t r, uint32_t w) {
-      return ((W(r, w)[0] >> 6) & 3u) > 1 ? r * wpc + (w / 3) * 3 : r * wpc + w;
+      return ((W(r, w)[0] >> 7) & 3u) > 1 ? r * wpc + (w / 3) * 3 : r * wpc + w;
     };
     std::vector<Z> st((size_t)K * groups * stage, Z{0, 0});
     std::vector<int> owner(st.size(), -1);
     std::set<uint64_t> gathered;
     for (uint32_t r = 0; r < K; ++r)
       for (uint32_t g = 0; g < groups; ++g) {
-        const uint32_t h0 = W(r, 3 * g)[0], tw0 = (h0 >> 6) & 3u;
+        const uint32_t h0 = W(r, 3 * g)[0], tw0 = (h0 >> 7) & 3u;
         for (uint32_t i = 0; i < 3; ++i) {
-          const uint32_t h = W(r, 3 * g + i)[0], tw = (h >> 6) & 3u;
-          if (tw0 > 1 && i < tw0) bad += tw != tw0 || ((h >> 8) & 0xffu) != ((h0 >> 8) & 0xffu);
+          const uint32_t h = W(r, 3 * g + i)[0], tw = (h >> 7) & 3u;
+          if (tw0 > 1 && i < tw0) bad += tw != tw0 || ((h >> 9) & 0xffu) != ((h0 >> 9) & 0xffu);
           else bad += tw > 1;
-          if (tw) bad += ((h >> 8) & 0xffu) != levels || W(r, 3 * g + i)[1] != op0;
-          bad += (h & 63u) > 32 || (!tw && (h & 63u));
+          if (tw) bad += ((h >> 9) & 0xffu) != levels || W(r, 3 * g + i)[1] != op0;
+          bad += (h & 127u) > kMixWarpAmps || (!tw && (h & 127u));
         }
       }
     for (uint32_t r = 0; r < K; ++r)
       for (uint32_t w = 0; w < wpc; ++w) {
         const uint32_t* p = W(r, w);
-        const uint32_t nel = ((p[0] >> 6) & 3u) ? p[0] & 63u : 0u;
+        const uint32_t nel = ((p[0] >> 7) & 3u) ? p[0] & 127u : 0u;
         for (uint32_t l = 0; l < nel; ++l) {
           const uint32_t gw = p[kMixWpHeader + l], row = gw & 2047u, col = (gw >> 11) & 2047u, si = gw >> 22;
           if (row >= Ca || col >= Cb || si >= stage) {
@@ -170,10 +170,10 @@ extern "C" int mix_units_check(unsigned M, unsigned na, unsigned nb, const qpe_t
         uint32_t quads = 0;
         for (uint32_t w = 0; w < wpc; ++w) {
           const uint32_t* p = W(r, w);
-          if (!((p[0] >> 6) & 3u)) continue;
+          if (!((p[0] >> 7) & 3u)) continue;
           const size_t base = ((size_t)r * groups + w / 3) * stage;
           for (uint32_t u = 0; u < 8; ++u) {
-            const uint32_t uw = p[kMixWpHeader + 32 + 8 * lv + u];
+            const uint32_t uw = p[kMixWpHeader + kMixWarpAmps + 8 * lv + u];
             if (!((uw >> 21) & 1u)) continue;
             ++quads;
             const uint32_t li = uw & 1023u, ri = (uw >> 10) & 1023u;
@@ -191,7 +191,7 @@ extern "C" int mix_units_check(unsigned M, unsigned na, unsigned nb, const qpe_t
     for (uint32_t r = 0; r < K; ++r)
       for (uint32_t w = 0; w < wpc; ++w) {
         const uint32_t* p = W(r, w);
-        const uint32_t nel = ((p[0] >> 6) & 3u) ? p[0] & 63u : 0u;
+        const uint32_t nel = ((p[0] >> 7) & 3u) ? p[0] & 127u : 0u;
         for (uint32_t l = 0; l < nel; ++l) {
           const uint32_t gw = p[kMixWpHeader + l];
           if ((gw & 2047u) < Ca && ((gw >> 11) & 2047u) < Cb && (gw >> 22) < stage)
