@@ -380,17 +380,26 @@ __device__ __forceinline__ void group_line_ops(const DevOp* __restrict__ ops, co
   while (i < n) {
     // Set up the next run of up to kLineChunk terms that are skipped or have one
     // inline update per lane; stop before the first other term.
+    // The chunk's first descriptor words are loaded together (indices clamped
+    // to the pass), so that its setup waits on one shared-memory round trip
+    // for them and one for the entries, not on one chain per term.
     Item its[kLineChunk];
     bool has[kLineChunk];
     uint32_t m = 0;
     bool stop = false;
+    uint4 da[kLineChunk];
+#pragma unroll
+    for (uint32_t k = 0; k < kLineChunk; ++k) {
+      const uint32_t ik = min(i + k, n - 1);
+      da[k] = ldm<G>(reinterpret_cast<const uint4*>(ops + (rev ? op1 - 1 - ik : op0 + ik)));
+    }
 #pragma unroll
     for (uint32_t k = 0; k < kLineChunk; ++k) {
       has[k] = false;
       its[k] = Item{scr, (R)0, (R)0, 1u, false};
       if (!stop && i + k < n) {
-        uint4 a, b;
-        desc(i + k, a, b);
+        const uint4 a = da[k];
+        const uint4 b = ldm<G>(reinterpret_cast<const uint4*>(ops + (rev ? op1 - 1 - (i + k) : op0 + (i + k))) + 1);
         const uint32_t kind = a.z & 0xffu;
         const uint32_t count = kind == OPK_DIAG_ALL ? L : a.y;
         if (!cond(a.z) || count == 0) {
