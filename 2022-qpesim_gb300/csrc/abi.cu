@@ -459,6 +459,39 @@ static bool ensure_mix_units(const qpe_program* pr, uint32_t K, uint32_t wpc, ui
   return mu.scheduled > 0;
 }
 
+// The per-line programs of the row and column passes of `pr` for this geometry
+// and number of replicas, built on first use from the device's index pool and
+// line strings and kept with the program. False if no pass has programs.
+static bool ensure_line_units(const qpe_program* pr, uint32_t K, uint32_t wpc, uint32_t stage, uint32_t Rk,
+                              uint32_t replicas) {
+  const uint32_t key[5] = {K, wpc, stage, Rk, replicas};
+  if (std::equal(key, key + 5, pr->line_key)) return pr->line_passes > 0;
+  const HostProgram& hp = pr->hp;
+  cudaStream_t s = pr->ctx->stream;
+  std::vector<uint32_t> pool(hp.pool_words), strA(hp.Ca), strB(hp.Cb);
+  QPE_CK(cudaMemcpyAsync(pool.data(), pr->pool.p, pool.size() * 4, cudaMemcpyDeviceToHost, s));
+  QPE_CK(cudaMemcpyAsync(strA.data(), pr->strA.p, strA.size() * 4, cudaMemcpyDeviceToHost, s));
+  QPE_CK(cudaMemcpyAsync(strB.data(), pr->strB.p, strB.size() * 4, cudaMemcpyDeviceToHost, s));
+  QPE_CK(cudaStreamSynchronize(s));
+  LineUnits lu;
+  build_line_units(hp, pool.data(), strA.data(), strB.data(), K, wpc, Rk, replicas, stage, lu);
+  pr->line_words.release();
+  pr->line_offs.release();
+  pr->line_slot.release();
+  if (lu.passes) {
+    pr->line_words.alloc(lu.words.size() * 4);
+    pr->line_offs.alloc(lu.offs.size() * 4);
+    pr->line_slot.alloc(lu.pass_slot.size() * 4);
+    QPE_CK(cudaMemcpyAsync(pr->line_words.p, lu.words.data(), lu.words.size() * 4, cudaMemcpyHostToDevice, s));
+    QPE_CK(cudaMemcpyAsync(pr->line_offs.p, lu.offs.data(), lu.offs.size() * 4, cudaMemcpyHostToDevice, s));
+    QPE_CK(cudaMemcpyAsync(pr->line_slot.p, lu.pass_slot.data(), lu.pass_slot.size() * 4, cudaMemcpyHostToDevice, s));
+    QPE_CK(cudaStreamSynchronize(s));
+  }
+  std::copy(key, key + 5, pr->line_key);
+  pr->line_passes = lu.passes;
+  return lu.passes > 0;
+}
+
 static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint32_t first, uint32_t last,
                          bool exact, bool in_place = false, uint32_t mode = 0, uint32_t replicas = 1) {
   ResidentLaunch rl;
@@ -482,6 +515,12 @@ static void run_resident(qpe_state* st, const qpe_program* pr, uint32_t K, uint3
     ri.mix_words = pr->mix_words.as<uint32_t>();
     ri.mix_slot = pr->mix_slot.as<uint32_t>();
     ri.mix_wp_words = pr->mix_wp_words;
+  }
+  if (mode == 4 && K > 1 &&
+      ensure_line_units(pr, K, rl.warps_per_cta, rl.stage_elems, ri.rows_per_cta, std::max(replicas, 1u))) {
+    ri.line_slot = pr->line_slot.as<uint32_t>();
+    ri.line_offs = pr->line_offs.as<uint32_t>();
+    ri.line_words = pr->line_words.as<uint32_t>();
   }
   ri.state = st->data.p;
   ri.pool = pr->pool.as<uint32_t>();

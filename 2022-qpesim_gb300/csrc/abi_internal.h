@@ -79,6 +79,10 @@ struct qpe_program {
   // CTA, stage) and kept: mix_slot per pass, mix_words the warp programs.
   mutable qpe::DevBuf mix_words, mix_slot;
   mutable uint32_t mix_K = 0, mix_wpc = 0, mix_stage = 0, mix_wp_words = 0, mix_scheduled = 0;
+  // Per-line programs of the row and column passes (mix_units.h) for one
+  // geometry (cluster, warps per CTA, stage, rows per CTA, replicas).
+  mutable qpe::DevBuf line_words, line_offs, line_slot;
+  mutable uint32_t line_key[5] = {0, 0, 0, 0, 0}, line_passes = 0;
 };
 
 namespace qpe {

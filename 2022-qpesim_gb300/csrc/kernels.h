@@ -136,6 +136,13 @@ struct ResidentInstance {
   void* xbuf;
   uint32_t* xflag;
   int* err;
+  // Row and column passes as per-line programs (mix_units.h, k_resident_lean
+  // with a cluster > 1): per pass its block of program offsets or
+  // kMixNoSchedule, the offsets ([block][replica][cta][warp]) and the programs.
+  // line_slot == nullptr: every row and column pass by the line runner.
+  const uint32_t* line_slot;
+  const uint32_t* line_offs;
+  const uint32_t* line_words;
 };
 constexpr int kResidentErrExchange = 4;
 struct ResidentLaunch {

@@ -327,4 +327,116 @@ bool build_mix_units(const HostProgram& hp, const uint32_t* pool, uint32_t K, ui
   return true;
 }
 
+bool build_line_units(const HostProgram& hp, const uint32_t* pool, const uint32_t* strA, const uint32_t* strB,
+                      uint32_t K, uint32_t warps_per_cta, uint32_t rows_per_cta, uint32_t replicas,
+                      uint32_t stage_elems, LineUnits& out) {
+  out = LineUnits{};
+  out.replicas = replicas = std::max(replicas, 1u);
+  out.pass_slot.assign(hp.passes.size(), kMixNoSchedule);
+  const uint32_t groups = warps_per_cta / kMaxTeam, Ca = (uint32_t)hp.Ca, Cb = (uint32_t)hp.Cb;
+  if (K < 2 || groups == 0 || Ca >= kLineLimit || Cb >= kLineLimit) return false;
+  const size_t block = (size_t)replicas * K * warps_per_cta;
+  constexpr uint32_t kLevelWords = 1 + kQuads, kTeam = kMaxTeam;
+  constexpr uint32_t kPairCap = kTeam * kQuads, kDiagCap = kTeam * 2 * kQuads;  // updates per level
+  for (size_t pi = 0; pi < hp.passes.size(); ++pi) {
+    const Pass& ps = hp.passes[pi];
+    if (ps.type == PASS_MIX || ps.op1 <= ps.op0) continue;
+    const bool col = ps.type == PASS_COL;
+    const uint32_t lines = col ? Cb : Ca, L = col ? Ca : Cb;
+    if (L > kTeam * kLanes || L > stage_elems || L > kIdxLimit) continue;
+    bool ok = true;
+    for (uint32_t k = ps.op0; k < ps.op1 && ok; ++k) ok = hp.ops[k].gen == OP_INLINE;
+    if (!ok) continue;
+    std::vector<uint32_t> offs(block, kMixNoSchedule);
+    std::vector<uint32_t> words;
+    const size_t base = out.words.size();
+    for (uint32_t ln = 0; ln < lines && ok; ++ln) {
+      // the line's replica, CTA and group
+      uint32_t r, cta, g;
+      if (col) {
+        r = ln % replicas;
+        const uint32_t j = ln / replicas;
+        cta = j % K;
+        g = j / K;
+      } else {
+        cta = ln / rows_per_cta;
+        const uint32_t t = ln - cta * rows_per_cta;
+        r = t % replicas;
+        g = t / replicas;
+      }
+      if (g >= groups || cta >= K) {
+        ok = false;
+        break;
+      }
+      const uint32_t lstr = col ? strB[ln] : strA[ln];
+      // levels: (op word, update slots)
+      std::vector<uint32_t> lev;  // kTeam * kLevelWords words per level: warp w's op word and 8 update words
+      auto new_level = [&](uint32_t opw) {
+        const size_t at = lev.size();
+        lev.resize(at + kTeam * kLevelWords, 0u);
+        for (uint32_t w = 0; w < kTeam; ++w) lev[at + w * kLevelWords] = opw;
+        return at;
+      };
+      for (uint32_t k = ps.op0; k < ps.op1; ++k) {
+        const DevOp& d = hp.ops[k];
+        uint32_t m = 0;
+        if (d.ncond > 0) m |= 1u << d.cb0;
+        if (d.ncond > 1) m |= 1u << d.cb1;
+        if ((lstr & m) != m) continue;  // the term does not act on this line
+        const uint32_t count = d.kind == OPK_DIAG_ALL ? L : d.count;
+        if (count == 0) continue;
+        const uint32_t op = k - ps.op0;  // index within the pass: the kernel reverses it
+        if (d.kind == OPK_PAIR) {
+          for (uint32_t j0 = 0; j0 < count; j0 += kPairCap) {
+            const size_t at = new_level(op);
+            for (uint32_t j = j0; j < std::min(count, j0 + kPairCap); ++j) {
+              const uint32_t w0 = pool[d.tab + 2 * j], a01 = w0 & 0x7fffffffu, a10 = pool[d.tab + 2 * j + 1];
+              if (a01 >= L || a10 >= L) ok = false;
+              const uint32_t s = j - j0;
+              lev[at + (s / kQuads) * kLevelWords + 1 + s % kQuads] =
+                  a01 | (a10 << 10) | ((w0 >> 31) << 20) | (1u << 21);
+            }
+          }
+        } else {
+          for (uint32_t j0 = 0; j0 < count; j0 += kDiagCap) {
+            const size_t at = new_level(op | 0x80000000u);
+            for (uint32_t j = j0; j < std::min(count, j0 + kDiagCap); ++j) {
+              const uint32_t e = d.kind == OPK_DIAG_LIST ? pool[d.tab + j] : j;
+              if (e >= L) ok = false;
+              const uint32_t s = j - j0, w = s / (2 * kQuads), u = (s % (2 * kQuads)) / 2, half = s & 1u;
+              uint32_t& word = lev[at + w * kLevelWords + 1 + u];
+              word |= (e << (10 * half)) | (1u << (20 + half));
+            }
+          }
+        }
+      }
+      const uint32_t nlev = (uint32_t)(lev.size() / (kTeam * kLevelWords));
+      // the team's three programs
+      for (uint32_t w = 0; w < kTeam; ++w) {
+        const uint32_t off = (uint32_t)(base + words.size());
+        offs[((size_t)r * K + cta) * warps_per_cta + g * kTeam + w] = off;
+        const uint32_t e0 = w * kLanes, e1 = std::min(L, e0 + kLanes), nel = e1 > e0 ? e1 - e0 : 0u;
+        std::vector<uint32_t> prog(kMixWpHeader + kLanes + (size_t)nlev * kLevelWords, 0u);
+        prog[0] = nel | (kTeam << 7);
+        prog[1] = nlev;
+        for (uint32_t e = e0; e < e1; ++e) {
+          const uint32_t row = col ? e : ln, cc = col ? ln : e;
+          prog[kMixWpHeader + (e - e0)] = row | (cc << 11) | (e << 22);
+        }
+        for (uint32_t lv = 0; lv < nlev; ++lv)
+          std::copy_n(lev.data() + ((size_t)lv * kTeam + w) * kLevelWords, kLevelWords,
+                      prog.data() + kMixWpHeader + kLanes + (size_t)lv * kLevelWords);
+        // pad to 16 bytes
+        prog.resize((prog.size() + 3) & ~(size_t)3, 0u);
+        words.insert(words.end(), prog.begin(), prog.end());
+      }
+    }
+    if (!ok) continue;
+    out.pass_slot[pi] = out.passes++;
+    out.offs.insert(out.offs.end(), offs.begin(), offs.end());
+    out.words.insert(out.words.end(), words.begin(), words.end());
+  }
+  return out.passes > 0;
+}
+
 }  // namespace qpe

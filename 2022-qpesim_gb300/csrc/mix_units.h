@@ -65,6 +65,51 @@ uint32_t mix_wp_words(const HostProgram& hp);
 bool build_mix_units(const HostProgram& hp, const uint32_t* pool, uint32_t K, uint32_t warps_per_cta,
                      uint32_t stage_elems, uint32_t max_window, MixUnits& out);
 
+// Row and column passes as per-line programs (k_resident_lean, strategy 7).
+//
+// A row or column pass applies its terms to every line (row or column)
+// separately, in order, each term on the line only if the line's own string has
+// the term's condition orbitals. The host evaluates those conditions per line
+// and writes, for each line, the program of the terms that apply: one level per
+// term (a term whose updates exceed the team's lanes takes several levels, its
+// trips, which touch disjoint amplitudes), each with the term's op index and the
+// update word of every quad. The kernel then runs a line like an update unit: a
+// team of three warps gathers the line into its group's stage, runs the levels
+// (the next levels' words loaded ahead from global memory) and scatters it back,
+// with no per-term decisions on the device. Pair updates are the quad-split
+// updates of the line runner (left / right stage index, parity); diagonal
+// updates are split over lane pairs (two amplitudes per word, lane h writing
+// component h of v (c0 + i c1) as in the line runner).
+//
+// With replicas, line b of a column pass runs on replica b % replicas and row a
+// of a row pass on replica (a - first row of its CTA) % replicas: the lines
+// each replica exchanges afterwards. Rows run on the CTA that owns them.
+//
+// Line program (words):
+//   w[0]   nelem (bits 0-6) | team warps (bits 7-8)     w[1] levels
+//   w[kMixWpHeader + l]    gather entry l, as in a window's program
+//   w[kMixWpHeader + kMixWarpAmps + 9 k]       op index | diagonal << 31
+//   w[kMixWpHeader + kMixWarpAmps + 9 k + 1 + u]
+//          pair: left | right << 10 | parity << 20 | valid << 21
+//          diagonal: amplitude of slot 2u | of slot 2u + 1 << 10 | valid << 20 | valid << 21
+//     (quad u; for a diagonal level lanes 4u, 4u + 1 take slot 2u, lanes 4u + 2,
+//     4u + 3 slot 2u + 1)
+struct LineUnits {
+  uint32_t passes = 0;               // row and column passes with programs
+  uint32_t replicas = 1;
+  std::vector<uint32_t> pass_slot;   // per pass: its block of program offsets, or kMixNoSchedule
+  std::vector<uint32_t> offs;        // blocks [slot][replica][cta][warp]: word offset of the
+                                     // warp's program, or kMixNoSchedule (idle)
+  std::vector<uint32_t> words;
+};
+
+// Builds the line programs of every row and column pass of `hp` whose terms are
+// inline (general pair matrices keep the line runner). strA / strB: the line
+// strings by rank (the device's tables); pool: the index pool.
+bool build_line_units(const HostProgram& hp, const uint32_t* pool, const uint32_t* strA, const uint32_t* strB,
+                      uint32_t K, uint32_t warps_per_cta, uint32_t rows_per_cta, uint32_t replicas,
+                      uint32_t stage_elems, LineUnits& out);
+
 }  // namespace qpe
 
 #endif  // QPE_MIX_UNITS_H_

@@ -661,6 +661,73 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
             if (lane < nel) *gp = *sp;
             if (lane + 32 < nel) *gp2 = *sp2;
           }
+        } else if (K > 1 && I.line_slot && __ldg(I.line_slot + pi) != kMixNoSchedule) {
+          // a row or column pass as per-line programs (mix_units.h): this warp's
+          // share of its group's line, if it has one
+          const uint32_t off =
+              __ldg(I.line_offs + (((size_t)__ldg(I.line_slot + pi) * nrep_f() + rep_f()) * K + rank) * wpc + warp);
+          if (off != kMixNoSchedule) {
+            const uint32_t* const prog = I.line_words + off;
+            const uint32_t hdr = __ldg(prog), nlev = __ldg(prog + 1);
+            const uint32_t tw = (hdr >> 7) & 3u, nel = hdr & 127u;
+            auto tsync = [&]() {
+              if (tw == 1) __syncwarp();
+              else asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(32 * tw) : "memory");
+            };
+            C2* const gst = blk + (size_t)Rk * Cb + (size_t)grp * stage_elems;
+            const uint32_t gw = lane < nel ? __ldg(prog + kMixWpHeader + lane) : 0u;
+            const uint32_t gw2 = lane + 32 < nel ? __ldg(prog + kMixWpHeader + 32 + lane) : 0u;
+            C2* const gp = at(gw & 2047u, (gw >> 11) & 2047u);
+            C2* const sp = gst + (gw >> 22);
+            C2* const gp2 = at(gw2 & 2047u, (gw2 >> 11) & 2047u);
+            C2* const sp2 = gst + (gw2 >> 22);
+            if (lane < nel) {
+              const C2 v = *gp;
+              if (lane + 32 < nel) *sp2 = *gp2;
+              *sp = v;
+            }
+            tsync();
+            // levels: op word (index in the pass | diagonal << 31) and this quad's
+            // update word, streamed from global memory three levels ahead; the
+            // coefficients one level ahead
+            const uint32_t* const lw = prog + kMixWpHeader + kMixWarpAmps;
+            const uint32_t q = lane & 3u, quad = lane >> 2;
+            const bool side1 = q >= 2;
+            const uint32_t comp1 = q & 1u, sflip = comp1 ^ 1u, half = (lane >> 1) & 1u, hh = lane & 1u;
+            R* const gr = reinterpret_cast<R*>(gst);
+            auto at_lv = [&](uint32_t i) { return lw + 9 * (size_t)(rev ? nlev - 1 - i : i); };
+            uint32_t o0 = 0, u0 = 0, o1 = 0, u1 = 0, o2 = 0, u2 = 0;
+            if (nlev > 0) { o0 = __ldg(at_lv(0)); u0 = __ldg(at_lv(0) + 1 + quad); }
+            if (nlev > 1) { o1 = __ldg(at_lv(1)); u1 = __ldg(at_lv(1) + 1 + quad); }
+            if (nlev > 2) { o2 = __ldg(at_lv(2)); u2 = __ldg(at_lv(2) + 1 + quad); }
+            uint4 b_n = ldm<G>(reinterpret_cast<const uint4*>(ops + P.op0 + (o0 & 0xffffffu)) + 1);
+            for (uint32_t i = 0; i < nlev; ++i) {
+              const uint32_t opw = o0, uw = u0;
+              const uint4 b = b_n;
+              o0 = o1; u0 = u1; o1 = o2; u1 = u2;
+              if (i + 3 < nlev) { o2 = __ldg(at_lv(i + 3)); u2 = __ldg(at_lv(i + 3) + 1 + quad); }
+              if (i + 1 < nlev) b_n = ldm<G>(reinterpret_cast<const uint4*>(ops + P.op0 + (o0 & 0xffffffu)) + 1);
+              const R c = (R)__hiloint2double((int)b.y, (int)b.x), t = (R)__hiloint2double((int)b.w, (int)b.z);
+              if (opw >> 31) {
+                // diagonal: lanes 4u, 4u + 1 take the word's first amplitude, 4u + 2, 4u + 3 its second;
+                // lane h writes component h of v (c + i t)
+                const bool v = (uw >> (20 + half)) & 1u;
+                R* const dp = gr + 2 * ((uw >> (10 * half)) & 1023u) + hh;
+                const R x1 = v ? *dp : (R)0;
+                const R x2 = __shfl_xor_sync(0xffffffffu, x1, 1);
+                if (v) *dp = A::add(A::mul(x1, c), A::mul(x2, hh ? t : neg(t)));
+              } else {
+                const bool v = (uw >> 21) & 1u;
+                R* const dp = gr + 2 * (side1 ? ((uw >> 10) & 1023u) : (uw & 1023u)) + comp1;
+                const R x1 = v ? *dp : (R)0;
+                const R x2 = __shfl_xor_sync(0xffffffffu, x1, 3);
+                if (v) *dp = A::add(A::mul(x1, c), A::mul(x2, (((uw >> 20) & 1u) ^ sflip) ? neg(t) : t));
+              }
+              tsync();
+            }
+            if (lane < nel) *gp = *sp;
+            if (lane + 32 < nel) *gp2 = *sp2;
+          }
         } else if (P.type == PASS_ROW) {
           // this CTA's rows of this replica, one per group tile, in place
           const uint32_t nrep = nrep_f();

@@ -1,5 +1,5 @@
-"""The column-pair update-unit scheduler (csrc/mix_units.cpp, strategy 7), on the
-CPU: tests/units/mix_units_check.cc runs every scheduled window of a program both
+"""The column-pair update-unit scheduler and the row and column passes' per-line
+programs (csrc/mix_units.cpp, strategy 7), on the CPU: tests/units/mix_units_check.cc runs every scheduled window of a program both
 the tile runner's way and the warp programs' way on a random complex128 block and
 counts differences (bit for bit) and broken kernel invariants (team layout,
 bounds, one owner per stage index and per amplitude). The GPU parity tests run
@@ -28,6 +28,8 @@ def checker(tmp_path_factory):
     lib.mix_units_check.restype = C.c_int
     lib.mix_units_check.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_uint, C.c_uint,
                                     C.c_uint, C.c_uint, C.c_uint, C.POINTER(C.c_uint)]
+    lib.line_units_check.restype = C.c_int
+    lib.line_units_check.argtypes = lib.mix_units_check.argtypes
     return lib
 
 
@@ -68,3 +70,24 @@ def test_units_too_large_fall_back(q, checker):
     group, so no pass is scheduled and every column-pair pass keeps the tiles."""
     bad, st = _run(q, checker, 20, 16, 1, 15, 4)
     assert bad == 0 and st["scheduled"] == 0 and st["windows"] == 0
+
+
+@pytest.mark.parametrize("n,K,order,wpc,replicas", [(16, 16, 2, 15, 1), (16, 16, 2, 15, 5), (16, 16, 1, 15, 3),
+                                                    (12, 4, 2, 15, 2), (12, 16, 1, 9, 1), (14, 8, 1, 15, 2),
+                                                    (8, 2, 1, 15, 2)])
+def test_line_programs_equal_line_runs(q, checker, n, K, order, wpc, replicas):
+    """The row and column passes' per-line programs (conditions evaluated on the
+    host, terms split into levels of at most 24 pair or 48 diagonal updates)
+    give the line runner's results bit for bit, each line on the replica that
+    exchanges it and rows on the CTA that owns them."""
+    M, e = n // 2, n // 4
+    h = q.Hamiltonian.from_integrals(q.synthetic_integrals(n, n), e, 0.05)
+    seg = h.segmented_terms()
+    arrs = [np.ascontiguousarray(seg[k], dtype=q._native.TERM_DTYPE) for k in KINDS]
+    ptrs = (C.c_void_p * 5)(*[a.ctypes.data for a in arrs])
+    ns = (C.c_size_t * 5)(*[len(a) for a in arrs])
+    stats = (C.c_uint * 4)()
+    stage = max(2 * math.comb(M, e), 3 * 64)
+    bad = checker.line_units_check(M, e, e, ptrs, ns, order, K, wpc, stage, replicas, stats)
+    assert bad == 0
+    assert stats[0] > 0  # passes with programs
