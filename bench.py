@@ -350,7 +350,8 @@ def run_ours(args, w, rank, ws, local):
     lib = N.lib()
 
     def evolve():
-        st.evolve(prog, 1, 1 + npow, strategy=args.strategy, cluster_size=args.cluster)
+        st.evolve(prog, 1, 1 + npow, strategy=args.strategy, cluster_size=args.cluster,
+                  replicas=getattr(args, "replicas", 0))
 
     def step():
         evolve()
@@ -980,6 +981,8 @@ def main():
                          "5 cluster with column pairs by four-warp groups, 6 cluster of three-warp groups, "
                          "7 as 6 with column-pair passes as windows of update units")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per cluster for --strategy 2 (0: smallest)")
+    ap.add_argument("--replicas", type=int, default=0,
+                    help="replica clusters for --strategy 7 (0 or 1: one; the autotuner picks them with --strategy 0)")
     ap.add_argument("--powers", type=int, default=0,
                     help="evolve only the first K controlled powers (profiling runs; not a workload's figure)")
     ap.add_argument("--precision", type=int, default=0,
