@@ -234,11 +234,13 @@ int qpe_state_zero(qpe_state* st);
 #define QPE_STRATEGY_LEAN 6     /* as CLUSTER (cluster_size 1..16): every row, column or column
                                    pair processed by a three-warp group, pair updates split over
                                    four lanes and diagonal updates over two */
-#define QPE_STRATEGY_LEAN_UNITS 7 /* as LEAN (cluster_size 2..16), with each column-pair pass split
-                                     into the connected components of its row pairings per column
-                                     pair, packed into warps by a host schedule: no CTA runs two
-                                     column pairs while others idle, and a warp synchronises with
-                                     itself between terms instead of with its group */
+#define QPE_STRATEGY_LEAN_UNITS 7 /* as LEAN (cluster_size 2..16), with runs of column-pair passes
+                                     split into the connected components of their pairings
+                                     (update units) packed into warps by a host schedule, and the
+                                     row and column passes run as per-line programs whose term
+                                     conditions the host evaluated: no CTA runs two column pairs
+                                     while others idle, one gather, scatter and cluster barrier per
+                                     window of up to 8 passes, no per-term decisions on the device */
 
 /* complex128 only: allow fused multiply-adds. Results then differ from the
  * reference's rounding by a few ulps per update (within 1e-12 of it) instead of
