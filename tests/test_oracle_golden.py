@@ -128,8 +128,8 @@ def test_oracle_term_compiler_matches_reference(q, orc, name):
                                                   (12, 3, 2, 1, 1), (10, 1, 1, 2, 3), (20, 5, 5, 1, 1)])
 def test_oracle_touch_counts(q, orc, n, na, nb, order, steps):
     """Amplitude updates per controlled power counted from the oracle's run
-    tables: the survey's counts of the reference (n = 8: 2,160, n = 16: 3,038,000
-    per first-order step) and the product's program planner's counts."""
+    tables: the counts the reference's own loops give (n = 8: 2,160, n = 16:
+    3,038,000 per first-order step) and the product's program planner's counts."""
     ints = q.synthetic_integrals(n, 1)
     seg = orc.segmented_terms(n // 2, max(na, nb), 0.05, ints.one_body, ints.two_body)
     got = orc.touches_per_power(n // 2, na, nb, seg, order, steps)
