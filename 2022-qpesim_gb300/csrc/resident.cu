@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(480) k_resident_lean(const ResidentInstance* _
     }
     const bool failed = __syncthreads_or(late) || (xs & 1u);
     if (threadIdx.x == 0) {
-      if (late) atomicOr(I.err, kResidentErrExchange);
+      if (failed && !(xs & 1u)) atomicOr(I.err, kResidentErrExchange);  // the first wait of this CTA that ran out
       xstate = (xgen << 1) | (failed ? 1u : 0u);
     }
     for (uint32_t i = threadIdx.x; i < nown; i += blockDim.x)
