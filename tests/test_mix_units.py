@@ -91,3 +91,32 @@ def test_line_programs_equal_line_runs(q, checker, n, K, order, wpc, replicas):
     bad = checker.line_units_check(M, e, e, ptrs, ns, order, K, wpc, stage, replicas, stats)
     assert bad == 0
     assert stats[0] > 0  # passes with programs
+
+
+def test_general_matrices_keep_the_runners(q, checker):
+    """A pair term whose matrix is not of the inline form (m00 real, m01
+    imaginary) keeps its pass on the tile or line runner: the schedules leave
+    that pass out and stay exact for the rest."""
+    n, K = 12, 4
+    M, e = n // 2, n // 4
+    seg = {k: np.array(v, copy=True) for k, v in
+           q.Hamiltonian.from_integrals(q.synthetic_integrals(n, 3), e, 0.05).segmented_terms().items()}
+    pqrs, pq = seg["pqrs"], seg["pq"]
+    mixed = np.flatnonzero((pqrs["p"] < M) & (pqrs["s"] < M) & (pqrs["q"] >= M) & (pqrs["r"] >= M))
+    pqrs["even"][mixed[0], 1] = 1e-3  # m00 of one column-pair term gets an imaginary part
+    pq["odd"][0, 1] = 1e-3            # and m00 of one pq term
+    arrs = [np.ascontiguousarray(seg[k], dtype=q._native.TERM_DTYPE) for k in KINDS]
+    ptrs = (C.c_void_p * 5)(*[a.ctypes.data for a in arrs])
+    ns = (C.c_size_t * 5)(*[len(a) for a in arrs])
+    stage = max(2 * math.comb(M, e), 3 * 64)
+    s1, s2 = (C.c_uint * 4)(), (C.c_uint * 4)()
+    assert checker.mix_units_check(M, e, e, ptrs, ns, 1, K, 15, stage, 8, s1) == 0
+    assert checker.line_units_check(M, e, e, ptrs, ns, 1, K, 15, stage, 1, s2) == 0
+    clean = [np.ascontiguousarray(v, dtype=q._native.TERM_DTYPE) for v in
+             (q.Hamiltonian.from_integrals(q.synthetic_integrals(n, 3), e, 0.05).segmented_terms()[k] for k in KINDS)]
+    cp = (C.c_void_p * 5)(*[a.ctypes.data for a in clean])
+    c1, c2 = (C.c_uint * 4)(), (C.c_uint * 4)()
+    assert checker.mix_units_check(M, e, e, cp, ns, 1, K, 15, stage, 8, c1) == 0
+    assert checker.line_units_check(M, e, e, cp, ns, 1, K, 15, stage, 1, c2) == 0
+    assert s1[0] < c1[0]  # fewer column-pair passes scheduled
+    assert s2[0] < c2[0]  # fewer row / column passes with programs
