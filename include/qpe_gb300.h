@@ -196,7 +196,10 @@ typedef struct qpe_program_info {
  * (odd electron counts) the reference cannot represent.
  * trotter_order 1 = the reference's first-order sweep; 2 = symmetric (Strang)
  * product of a forward and a reversed sweep, each with the coefficients given
- * (compute them at half the step). steps_per_power repeats the step. */
+ * (compute them at half the step). steps_per_power repeats the step.
+ * A program keeps the schedules QPE_STRATEGY_LEAN_UNITS builds on first use
+ * (for one cluster, replica count and geometry at a time): evolve with one
+ * program from one host thread at a time. */
 int qpe_program_create(qpe_context* ctx, uint32_t num_orbitals, uint32_t n_alpha,
                        uint32_t n_beta, const qpe_term* pp, size_t n_pp, const qpe_term* pq,
                        size_t n_pq, const qpe_term* pqqp, size_t n_pqqp, const qpe_term* pqqr,
