@@ -120,3 +120,18 @@ def test_general_matrices_keep_the_runners(q, checker):
     assert checker.line_units_check(M, e, e, cp, ns, 1, K, 15, stage, 1, c2) == 0
     assert s1[0] < c1[0]  # fewer column-pair passes scheduled
     assert s2[0] < c2[0]  # fewer row / column passes with programs
+
+
+@pytest.mark.parametrize("n,na,nb,K,replicas", [(14, 4, 3, 8, 2), (12, 2, 4, 4, 1), (16, 3, 4, 16, 3)])
+def test_schedules_with_unequal_spins(q, checker, n, na, nb, K, replicas):
+    """Both schedules with different alpha and beta electron counts (rows and
+    columns of different lengths)."""
+    M = n // 2
+    seg = q.Hamiltonian.from_integrals(q.synthetic_integrals(n, 40 + n), max(na, nb), 0.05).segmented_terms()
+    arrs = [np.ascontiguousarray(seg[k], dtype=q._native.TERM_DTYPE) for k in KINDS]
+    ptrs = (C.c_void_p * 5)(*[a.ctypes.data for a in arrs])
+    ns = (C.c_size_t * 5)(*[len(a) for a in arrs])
+    stage = max(2 * math.comb(M, na), 3 * 64)
+    s1, s2 = (C.c_uint * 4)(), (C.c_uint * 4)()
+    assert checker.mix_units_check(M, na, nb, ptrs, ns, 2, K, 15, stage, 8, s1) == 0
+    assert checker.line_units_check(M, na, nb, ptrs, ns, 2, K, 15, stage, replicas, s2) == 0
